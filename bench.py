@@ -1,0 +1,448 @@
+#!/usr/bin/env python
+"""BCSR SpMV block-size sweep on GB300 — the benchmark line.
+
+Workload (one "step"): y = A x once for each of 12 matrices — the seeded
+random-band BCSR family with 100 000 block rows, 8 distinct block columns per
+block row drawn from a +-64 band, block sizes 1, 2, 4, 8, 16, 32, in FP64 and
+in FP32 (values and x uniform in [-1, 1)). Data are synthetic by
+construction: the reference has no dataset, only generated matrices.
+
+  value        algorithmic bytes of all 12 products / their summed device time
+               (CUDA events around each product on the launching stream), GB/s.
+               Bytes per product = values + 4-byte block columns + row offsets
+               + x read once + y written once.
+  L2           flushed before every product (write a 256 MB buffer, then read a
+               512 MB one so no dirty line is written back inside the timed
+               product); the flush is outside the events.
+  e2e          the same bytes over the wall time of the user-facing call path
+               with host buffers: bmfp_matrix_create_bcsr from pinned host
+               arrays (allocation + upload), x upload, bmfp_matrix_spmv, y
+               download, handle release — copies inside the timed region.
+  roofline     the dominant product (largest share of device time) against
+               MEASURED_PEAKS.json's HBM copy bandwidth.
+  cpu_baseline the oracle's restatement of the reference CPU loop
+               (main.cpp:36-45, one thread) on the first rows of every matrix.
+
+`--impl reference` times the reference's CPU path (the same loop, all host
+threads) on a bounded sample of the same sweep and prints the same metric.
+
+Multi-GPU: replicas only — every rank runs the whole sweep on its own GPU
+(no collective on the data path); value sums the ranks' bytes over the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NBR, BPR, HALF_BAND, SEED, X_STREAM = 100_000, 8, 64, 0, 2
+BLOCK_SIZES = (1, 2, 4, 8, 16, 32)
+DTYPES = ("f64", "f32")
+METRIC = "SpMV GB/s vs HBM peak"
+WORKLOAD = ("BCSR SpMV block-size sweep: 100000 block rows, 8 blocks/row drawn from a +-64 band, "
+            "bs 1,2,4,8,16,32, FP64 and FP32, x uniform in [-1,1)")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-csr-compare", action="store_true")
+    ap.add_argument("--sizes", default=",".join(map(str, BLOCK_SIZES)))
+    ap.add_argument("--dtypes", default=",".join(DTYPES))
+    return ap.parse_args()
+
+
+def np_dt(tag):
+    return np.float64 if tag == "f64" else np.float32
+
+
+def case_bytes(bs, tag, nnzb, nbr=NBR):
+    S = 8 if tag == "f64" else 4
+    return nnzb * bs * bs * S + nnzb * 4 + (nbr + 1) * 4 + 2 * nbr * bs * S
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi SM clock and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        mhz, mx, reasons = [], 0.0, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            p = [s.strip() for s in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                mhz.append(float(p[1]))
+                mx = max(mx, float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not mhz:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(mhz), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(mhz)}
+
+
+# ---------------------------------------------------------------- workload
+
+def build_cases(bm, sizes, dtypes, with_csr):
+    cases = []
+    for tag in dtypes:
+        for bs in sizes:
+            rp, c, v = bm.gen_band_bcsr(NBR, BPR, HALF_BAND, bs, SEED, np_dt(tag))
+            x = bm.gen_uniform_vector(NBR * bs, SEED, X_STREAM, np_dt(tag))
+            case = {"bs": bs, "tag": tag, "rp": rp, "c": c, "v": v, "x": x, "nnzb": int(c.size),
+                    "bytes": case_bytes(bs, tag, int(c.size))}
+            cases.append(case)
+    return cases
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def committed_traffic(kernel_key):
+    """dram bytes per launch of the dominant kernel from the committed ncu
+    summary (profiles/*.md line `traffic <key>: <bytes>`), or None."""
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return None
+    pat = re.compile(r"traffic\s+" + re.escape(kernel_key) + r"\s*:\s*([0-9.eE+]+)")
+    for f in sorted(os.listdir(pdir)):
+        if f.endswith((".md", ".txt")):
+            m = pat.search(open(os.path.join(pdir, f)).read())
+            if m:
+                return float(m.group(1))
+    return None
+
+
+def run_ours(args):
+    import torch
+
+    import block_matrix_format_performance_gb300 as bm
+    from block_matrix_format_performance_gb300 import build as B
+
+    rank, world, local = dist_env()
+    B.build()
+    bm.load()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    sizes = [int(s) for s in args.sizes.split(",")]
+    dtypes = args.dtypes.split(",")
+    t0 = time.time()
+    cases = build_cases(bm, sizes, dtypes, not args.no_csr_compare)
+    gen_s = time.time() - t0
+
+    stream = torch.cuda.current_stream()
+    for cs in cases:
+        cs["m"] = bm.Matrix.from_bcsr(cs["rp"], cs["c"], cs["v"], cs["bs"])
+        cs["dx"] = torch.from_numpy(cs["x"]).cuda()
+        cs["dy"] = torch.empty_like(cs["dx"])
+    flush_w = torch.empty(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB
+    flush_r = torch.ones(128 << 20, dtype=torch.float32, device="cuda")  # 512 MB
+
+    def flush():
+        flush_w.zero_()
+        flush_r.sum()
+
+    n = len(cases)
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(n)]
+    for _ in range(args.warmup):
+        for cs in cases:
+            flush()
+            cs["m"].spmv(cs["dx"], cs["dy"])
+    torch.cuda.synchronize()
+
+    per_case_ms = [0.0] * n
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            for i, cs in enumerate(cases):
+                flush()
+                ev[i][0].record(stream)
+                cs["m"].spmv(cs["dx"], cs["dy"])
+                ev[i][1].record(stream)
+            torch.cuda.synchronize()  # events of this step are complete
+            for i in range(n):
+                per_case_ms[i] += ev[i][0].elapsed_time(ev[i][1])
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    if dist:
+        dist.barrier()
+
+    step_ms = sum(per_case_ms) / args.steps
+    total_bytes = sum(cs["bytes"] for cs in cases)
+    t_max = step_ms
+    if dist:
+        t = torch.tensor([step_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = world * total_bytes / (t_max * 1e-3) / 1e9
+
+    per_case = {}
+    for i, cs in enumerate(cases):
+        ms = per_case_ms[i] / args.steps
+        per_case[f"bs{cs['bs']}_{cs['tag']}"] = {"gbs": round(cs["bytes"] / (ms * 1e-3) / 1e9, 1),
+                                                  "us": round(ms * 1e3, 2), "mb": round(cs["bytes"] / 1e6, 1)}
+    dom = max(range(n), key=lambda i: per_case_ms[i])
+    dcs = cases[dom]
+    dom_ms = per_case_ms[dom] / args.steps
+    hbm, peak_kind = peaks()
+    achieved = dcs["bytes"] / (dom_ms * 1e-3) / 1e9
+    dom_key = f"bcsr_native_bs{dcs['bs']}_{dcs['tag']}"
+    traffic = committed_traffic(dom_key)
+
+    # CSR warp-per-row ("GPU CSR-Vector") on the same matrices, for comparison.
+    csr_cmp = {}
+    if not args.no_csr_compare:
+        for cs in cases:
+            crp, cc, cv = bm.bcsr_to_csr(cs["rp"], cs["c"], cs["v"], cs["bs"])
+            d_rp, d_c, d_v = (torch.from_numpy(a).cuda() for a in (crp, cc, cv))
+            cbytes = bm.csr_spmv_bytes(np_dt(cs["tag"]), NBR * cs["bs"], NBR * cs["bs"], cc.size)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            reps, tot = 5, 0.0
+            for r in range(reps + 1):
+                flush()
+                e0.record(stream)
+                bm.csr_spmv(bm.CSR_VECTOR, d_rp, d_c, d_v, cs["dx"], cs["dy"])
+                e1.record(stream)
+                torch.cuda.synchronize()
+                if r:
+                    tot += e0.elapsed_time(e1)
+            ms = tot / reps
+            csr_cmp[f"bs{cs['bs']}_{cs['tag']}"] = {
+                "csr_vector_gbs": round(cbytes / (ms * 1e-3) / 1e9, 1),
+                "csr_vector_us": round(ms * 1e3, 2),
+                "native_speedup": round(ms / (per_case_ms[cases.index(cs)] / args.steps), 2)}
+            del d_rp, d_c, d_v
+
+    # End to end through the C ABI with host buffers.
+    pinned = []
+    for cs in cases:
+        pinned.append(tuple(torch.from_numpy(a).pin_memory() for a in (cs["rp"], cs["c"], cs["v"], cs["x"])))
+    h_y = [torch.empty(cs["x"].shape, dtype=torch.float64 if cs["tag"] == "f64" else torch.float32).pin_memory()
+           for cs in cases]
+    for cs in cases:
+        cs["m"].close()
+    h2d = sum(sum(t.numel() * t.element_size() for t in p) for p in pinned)
+    d2h = sum(t.numel() * t.element_size() for t in h_y)
+
+    def e2e_step():
+        for cs, p, hy in zip(cases, pinned, h_y):
+            m = bm.Matrix.from_bcsr(p[0].numpy(), p[1].numpy(), p[2].numpy(), cs["bs"])
+            dx = p[3].to("cuda", non_blocking=True)
+            dy = torch.empty_like(dx)
+            m.spmv(dx, dy)
+            hy.copy_(dy, non_blocking=True)
+            torch.cuda.synchronize()
+            m.close()
+
+    e2e_step()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - e0) / args.e2e_steps
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * total_bytes / e2e_s / 1e9
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(cases)
+
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_max, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "+".join(dtypes), "data": "synthetic (seeded generator; the reference has no dataset)",
+        "config": {
+            "workload": WORKLOAD, "n_block_rows": NBR, "blocks_per_row": BPR, "half_band": HALF_BAND,
+            "block_sizes": sizes, "seed": SEED, "parallelism": f"replicas x{world} (no collective)",
+            "l2": "flushed before every product (256 MB write + 512 MB read), outside the timed events",
+            "kernel": "GPU BCSR (GB300 native)", "per_case": per_case, "csr_warp_per_row": csr_cmp,
+            "wall_s_timed_region": round(wall, 3), "generate_s": round(gen_s, 1),
+        },
+        "roofline": {"bound": "hbm", "kernel": dom_key, "achieved": round(achieved, 1), "peak": hbm,
+                     "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                     else "fallback 6.8 TB/s", "unit": "GB/s", "frac": round(achieved / hbm, 4),
+                     "traffic": traffic, "algorithmic_bytes": dcs["bytes"]},
+        "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "s_per_step": round(e2e_s, 4)},
+        "gpu_launches": args.steps * n,
+        "clocks": clocks.summary(),
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+# ------------------------------------------------------------- CPU sides
+
+def cpu_sample(bm, cs, rows):
+    """First `rows` block rows of a case as CSR (the reference's CPU input)."""
+    rp = cs["rp"][:rows + 1].copy()
+    nnzb = int(rp[-1])
+    bs = cs["bs"]
+    crp, cc, cv = bm.bcsr_to_csr(rp, cs["c"][:nnzb], cs["v"][:nnzb * bs * bs], bs)
+    return crp, cc, cv, case_bytes(bs, cs["tag"], nnzb, rows)
+
+
+def cpu_baseline(cases, rows=20_000, reps=3):
+    """Oracle restatement of main.cpp:36-45 (one thread) on a bounded sample."""
+    import block_matrix_format_performance_gb300 as bm
+    from oracle import oracle as orc
+    tot_b, tot_s = 0, 0.0
+    for cs in cases:
+        crp, cc, cv, b = cpu_sample(bm, cs, rows)
+        x = cs["x"]
+        orc.csr_spmv(crp, cc, cv, x)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            orc.csr_spmv(crp, cc, cv, x)
+        tot_s += (time.perf_counter() - t0) / reps
+        tot_b += b
+    return {"value": round(tot_b / tot_s / 1e9, 2), "unit": "GB/s", "cores": 1, "kind": "port",
+            "sample": f"first {rows} of {NBR} block rows of each of the {len(cases)} sweep matrices, CSR, "
+                      f"{reps} passes; the reference CPU loop main.cpp:36-45 restated in C (-O2)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import block_matrix_format_performance_gb300 as bm
+    from block_matrix_format_performance_gb300 import build as B
+    from oracle import oracle as orc
+    B.build()
+    orc.build()
+    threads = os.cpu_count() or 1
+    sizes = [int(s) for s in args.sizes.split(",")]
+    dtypes = args.dtypes.split(",")
+    rows = 25_000
+    samples, tot_b = [], 0
+    for tag in dtypes:
+        for bs in sizes:
+            r = rows if bs < 32 else rows // 2
+            rp, c, v = bm.gen_band_bcsr(NBR, BPR, HALF_BAND, bs, SEED, np_dt(tag))
+            x = bm.gen_uniform_vector(NBR * bs, SEED, X_STREAM, np_dt(tag))
+            crp, cc, cv, b = cpu_sample(bm, {"rp": rp, "c": c, "v": v, "bs": bs, "tag": tag}, r)
+            del rp, c, v
+            samples.append((crp, cc, cv, x))
+            tot_b += b
+    for _ in range(args.warmup):
+        for s in samples:
+            orc.csr_spmv(*s, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for s in samples:
+            orc.csr_spmv(*s, threads=threads)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = tot_b / dt / 1e9
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "+".join(dtypes), "data": "synthetic (seeded generator)",
+        "impl": "reference",
+        "config": {"workload": WORKLOAD, "block_sizes": sizes, "sample_rows": rows},
+        "cpu_baseline": {"value": round(value, 2), "unit": "GB/s", "cores": threads, "kind": "port",
+                         "sample": f"first {rows} block rows (bs 32: {rows // 2}) of every sweep matrix as CSR; "
+                                   "the reference CPU loop main.cpp:36-45 restated in C, rows split over "
+                                   f"{threads} threads (the reference's main.cpp needs the absent fmt and "
+                                   "cuda_jit submodules, so it is not built)"},
+        "e2e": {"value": round(value, 2), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

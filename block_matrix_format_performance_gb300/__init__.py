@@ -1,0 +1,286 @@
+"""GB300-native block-sparse SpMV and BiCGStab — Python front end.
+
+The product is ``libbmfp.so`` (CUDA kernels for sm_103a behind the C ABI in
+``include/bmfp.h``) and the C++ headers in ``include/bmfp/`` that rebuild the
+reference's host API. This module is a thin ctypes layer used by the tests and
+the benchmark: numpy arrays for host data, torch CUDA tensors for device
+memory and streams. Every device call goes through the C ABI; there is no
+Python or CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from ._capi import BmfpError, check, load, LIB_PATH  # noqa: F401
+
+R32F, R64F = 0, 1
+
+# enum bmfp_spmv_variant (include/bmfp.h)
+CSR_SCALAR, CSR_VECTOR, CSR_NATIVE = 0, 1, 2
+BCSR_ROW_THREAD, BCSR_ROW_WARP = 3, 4
+BCSR_COL_THREAD, BCSR_COL_THREAD_TEMPLATE = 5, 6
+BCSR_COL_COAL_X, BCSR_COL_COAL_X_TEMPLATE = 7, 8
+BCSR_COL_BY_COL, BCSR_COL_BY_COL_FASTDIV, BCSR_COL_BY_COL_PO2, BCSR_COL_BY_COL_TEMPLATE = 9, 10, 11, 12
+BCSR_JIT, CUSPARSE_ROW, CUSPARSE_COL, BCSR_NATIVE = 13, 14, 15, 16
+VARIANT_COUNT = 17
+
+SUCCESS, ERROR_INVALID_VALUE, ERROR_CUDA, ERROR_OUT_OF_MEMORY, ERROR_NOT_SUPPORTED = 0, 1, 2, 3, 4
+ERROR_BREAKDOWN, ERROR_NOT_CONVERGED, ERROR_TIMEOUT, ERROR_BUDGET, PENDING = 5, 6, 7, 8, 9
+
+
+def dtype_enum(dtype) -> int:
+    dt = np.dtype(dtype) if not hasattr(dtype, "is_floating_point") else dtype
+    name = str(dt).replace("torch.", "")
+    if name in ("float64", "double"):
+        return R64F
+    if name in ("float32", "float"):
+        return R32F
+    raise TypeError(f"unsupported dtype {dtype}")
+
+
+def np_dtype(enum: int):
+    return np.float64 if enum == R64F else np.float32
+
+
+def _p(a):
+    """Raw pointer of a numpy array, torch tensor or int (None -> NULL)."""
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()  # torch tensor
+
+
+def _stream(stream):
+    if stream is None:
+        try:
+            import torch
+            if torch.cuda.is_available():
+                return torch.cuda.current_stream().cuda_stream
+        except Exception:  # pragma: no cover
+            pass
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+def variant_name(v: int) -> str:
+    s = load().bmfp_spmv_variant_name(v)
+    return s.decode() if s else None
+
+
+def variant_layout(v: int) -> int:
+    return load().bmfp_spmv_variant_layout(v)
+
+
+def variant_is_csr(v: int) -> int:
+    return load().bmfp_spmv_variant_is_csr(v)
+
+
+def device_count() -> int:
+    return load().bmfp_device_count()
+
+
+# ----------------------------------------------------------- host utilities
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def gen_n_diag_bcsr(n_rows, blocks_per_row, bs, dtype=np.float64):
+    """The reference's band generator (common/matrix_converters.h:157-196)."""
+    L = load()
+    rp = np.zeros(n_rows + 1, np.int32)
+    c = np.zeros(n_rows * blocks_per_row, np.int32)
+    v = np.zeros(n_rows * blocks_per_row * bs * bs, dtype)
+    check(L.bmfp_gen_n_diag_bcsr(dtype_enum(dtype), n_rows, blocks_per_row, bs, _p(rp), _p(c), _p(v)))
+    return rp, c, v
+
+
+def gen_band_bcsr(n_block_rows, blocks_per_row, half_band, bs, seed, dtype=np.float64):
+    """Seeded random-band BCSR (the block-size sweep workload)."""
+    L = load()
+    e = dtype_enum(dtype)
+    rp = np.zeros(n_block_rows + 1, np.int32)
+    nnzb = ctypes.c_int64(0)
+    check(L.bmfp_gen_band_bcsr(e, n_block_rows, blocks_per_row, half_band, bs, seed, _p(rp),
+                               ctypes.byref(nnzb), None, None))
+    c = np.zeros(nnzb.value, np.int32)
+    v = np.zeros(nnzb.value * bs * bs, dtype)
+    check(L.bmfp_gen_band_bcsr(e, n_block_rows, blocks_per_row, half_band, bs, seed, _p(rp),
+                               ctypes.byref(nnzb), _p(c), _p(v)))
+    return rp, c, v
+
+
+def gen_uniform_vector(n, seed, stream, dtype=np.float64):
+    out = np.zeros(n, dtype)
+    check(load().bmfp_gen_uniform_vector(dtype_enum(dtype), n, seed, stream, _p(out)))
+    return out
+
+
+def gen_q4_elasticity(nx, ny, dtype=np.float64, young=1.0, poisson=0.3):
+    """Q4 plane-stress stiffness (BCSR bs=2) and load for an nx*ny node grid."""
+    L = load()
+    e = dtype_enum(dtype)
+    rp = np.zeros(nx * ny + 1, np.int32)
+    nnzb = ctypes.c_int64(0)
+    check(L.bmfp_gen_q4_elasticity(e, nx, ny, young, poisson, _p(rp), ctypes.byref(nnzb), None, None, None))
+    c = np.zeros(nnzb.value, np.int32)
+    v = np.zeros(nnzb.value * 4, dtype)
+    rhs = np.zeros(2 * nx * ny, dtype)
+    check(L.bmfp_gen_q4_elasticity(e, nx, ny, young, poisson, _p(rp), ctypes.byref(nnzb), _p(c), _p(v),
+                                   _p(rhs)))
+    return rp, c, v, rhs
+
+
+def bcsr_to_csr(row_ptr, cols, vals, bs):
+    vals = np.ascontiguousarray(vals).reshape(-1)
+    row_ptr = _i32(row_ptr)
+    nbr = row_ptr.size - 1
+    nnz = int(row_ptr[-1]) * bs * bs
+    rp = np.zeros(nbr * bs + 1, np.int32)
+    c = np.zeros(nnz, np.int32)
+    v = np.zeros(nnz, vals.dtype)
+    check(load().bmfp_bcsr_to_csr(dtype_enum(vals.dtype), nbr, bs, _p(row_ptr), _p(_i32(cols)), _p(vals),
+                                  _p(rp), _p(c), _p(v)))
+    return rp, c, v
+
+
+def csr_to_bcsr(row_ptr, cols, vals, n_cols, bs):
+    L = load()
+    vals = np.ascontiguousarray(vals)
+    row_ptr, cols = _i32(row_ptr), _i32(cols)
+    n_rows = row_ptr.size - 1
+    e = dtype_enum(vals.dtype)
+    brp = np.zeros(n_rows // bs + 1, np.int32)
+    nnzb = ctypes.c_int64(0)
+    check(L.bmfp_csr_to_bcsr(e, n_rows, n_cols, bs, _p(row_ptr), _p(cols), _p(vals), _p(brp),
+                             ctypes.byref(nnzb), None, None))
+    bc = np.zeros(nnzb.value, np.int32)
+    bv = np.zeros(nnzb.value * bs * bs, vals.dtype)
+    check(L.bmfp_csr_to_bcsr(e, n_rows, n_cols, bs, _p(row_ptr), _p(cols), _p(vals), _p(brp),
+                             ctypes.byref(nnzb), _p(bc), _p(bv)))
+    return brp, bc, bv
+
+
+def transpose_blocks(row_ptr, vals, bs):
+    vals = np.ascontiguousarray(vals).reshape(-1)
+    row_ptr = _i32(row_ptr)
+    out = np.empty_like(vals)
+    check(load().bmfp_transpose_blocks(dtype_enum(vals.dtype), row_ptr.size - 1, bs, _p(row_ptr), _p(vals),
+                                       _p(out)))
+    return out
+
+
+def bcsr_spmv_bytes(dtype, n_block_rows, n_block_cols, bs, nnzb) -> int:
+    return load().bmfp_bcsr_spmv_bytes(dtype_enum(dtype), n_block_rows, n_block_cols, bs, nnzb)
+
+
+def csr_spmv_bytes(dtype, n_rows, n_cols, nnz) -> int:
+    return load().bmfp_csr_spmv_bytes(dtype_enum(dtype), n_rows, n_cols, nnz)
+
+
+# ------------------------------------------------------------ device calls
+
+def bcsr_spmv(variant, row_ptr, cols, vals, x, y, bs, n_block_cols=None, stream=None):
+    """y = A x through bmfp_bcsr_spmv; arrays are torch CUDA tensors."""
+    nbr = row_ptr.numel() - 1
+    nbc = n_block_cols if n_block_cols is not None else x.numel() // bs
+    check(load().bmfp_bcsr_spmv(dtype_enum(vals.dtype), variant, nbr, nbc, bs, cols.numel(), _p(row_ptr),
+                                _p(cols), _p(vals), _p(x), _p(y), _stream(stream)))
+    return y
+
+
+def bcsr_spmv_native(row_ptr, cols, vals, x, y, bs, lanes=0, stream=None):
+    check(load().bmfp_bcsr_spmv_native_ex(dtype_enum(vals.dtype), row_ptr.numel() - 1, bs, cols.numel(),
+                                          _p(row_ptr), _p(cols), _p(vals), _p(x), _p(y), lanes,
+                                          _stream(stream)))
+    return y
+
+
+def csr_spmv(variant, row_ptr, cols, vals, x, y, n_cols=None, stream=None):
+    n = row_ptr.numel() - 1
+    check(load().bmfp_csr_spmv(dtype_enum(vals.dtype), variant, n, n_cols if n_cols is not None else x.numel(),
+                               cols.numel(), _p(row_ptr), _p(cols), _p(vals), _p(x), _p(y), _stream(stream)))
+    return y
+
+
+def native_default_lanes(dtype, bs, avg_blocks_per_row) -> int:
+    return load().bmfp_bcsr_native_default_lanes(dtype_enum(dtype), bs, float(avg_blocks_per_row))
+
+
+class Matrix:
+    """Device-resident matrix handle (bmfp_matrix_t) uploaded from host arrays."""
+
+    def __init__(self, handle, dtype, n_rows, n_cols, bs, nnz):
+        self.handle = handle
+        self.dtype = dtype
+        self.n_rows, self.n_cols, self.bs, self.nnz = n_rows, n_cols, bs, nnz
+
+    @classmethod
+    def from_bcsr(cls, row_ptr, cols, vals, bs, n_block_cols=None, dtype=None, stream=None):
+        vals = np.ascontiguousarray(vals).reshape(-1)
+        if dtype is not None:
+            vals = vals.astype(dtype)
+        row_ptr, cols = _i32(row_ptr), _i32(cols)
+        nbr = row_ptr.size - 1
+        nbc = n_block_cols if n_block_cols is not None else nbr
+        h = ctypes.c_void_p()
+        e = dtype_enum(vals.dtype)
+        check(load().bmfp_matrix_create_bcsr(ctypes.byref(h), e, nbr, nbc, bs, cols.size, _p(row_ptr),
+                                             _p(cols), _p(vals), _stream(stream)))
+        return cls(h, e, nbr, nbc, bs, cols.size)
+
+    @classmethod
+    def from_csr(cls, row_ptr, cols, vals, n_cols, stream=None):
+        vals = np.ascontiguousarray(vals)
+        row_ptr, cols = _i32(row_ptr), _i32(cols)
+        h = ctypes.c_void_p()
+        e = dtype_enum(vals.dtype)
+        check(load().bmfp_matrix_create_csr(ctypes.byref(h), e, row_ptr.size - 1, n_cols, cols.size, _p(row_ptr),
+                                            _p(cols), _p(vals), _stream(stream)))
+        return cls(h, e, row_ptr.size - 1, n_cols, 0, cols.size)
+
+    def convert(self, dtype, stream=None):
+        h = ctypes.c_void_p()
+        e = dtype_enum(dtype)
+        check(load().bmfp_matrix_convert(ctypes.byref(h), self.handle, e, _stream(stream)))
+        return Matrix(h, e, self.n_rows, self.n_cols, self.bs, self.nnz)
+
+    @property
+    def rows(self):
+        return self.n_rows * (self.bs or 1)
+
+    @property
+    def cols(self):
+        return self.n_cols * (self.bs or 1)
+
+    def bytes_per_spmv(self) -> int:
+        b = ctypes.c_int64(0)
+        check(load().bmfp_matrix_info(self.handle, None, None, None, None, None, ctypes.byref(b)))
+        return b.value
+
+    def spmv(self, x, y, stream=None):
+        check(load().bmfp_matrix_spmv(self.handle, _p(x), _p(y), _stream(stream)))
+        return y
+
+    def autotune(self, x, y, stream=None) -> int:
+        g = ctypes.c_int(0)
+        check(load().bmfp_matrix_autotune(self.handle, _p(x), _p(y), _stream(stream), ctypes.byref(g)))
+        return g.value
+
+    def close(self):
+        if self.handle:
+            load().bmfp_matrix_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

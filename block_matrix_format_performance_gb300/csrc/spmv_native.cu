@@ -1,0 +1,461 @@
+// GB300-native sparse matrix-vector products.
+//
+// y = A x for BCSR with row-major bs x bs blocks (the layout of
+// common/matrix_converters.h:13-82) and for CSR. Both are HBM-bound streams:
+// every value and block column is read once, x is re-read from L1/L2 by the
+// neighbouring block rows, y is written once. The kernels are organised
+// around that:
+//
+//  * bcsr_flat_kernel (bs = 2, 4, 8, 16, 32): an aligned group of G lanes owns
+//    one block row. The block row's values are one contiguous run
+//    (row_ptr[i]*bs*bs .. row_ptr[i+1]*bs*bs) and the group walks it in
+//    16-byte vectors, lane l taking vector l of each G*16-byte chunk, so a
+//    warp-wide load is one fully used 512-byte stretch. Because bs*bs and the
+//    chunk are both powers of two, every lane keeps a fixed (row, column
+//    group) position inside a block (chunk >= block) or a fixed column group
+//    and a fixed set of rows per phase (chunk < block). Partial row sums are
+//    combined with xor-shuffles over exactly the lane bits that vary the
+//    column, so the reduction costs log2 steps and no shared memory.
+//  * bcsr_tpr_kernel (any bs <= 32, e.g. 3 for frame elements): a warp owns
+//    a block row, lane (q, r) takes scalar row r of blocks q, q+Q, ... with
+//    Q = 32/bs, then a shuffle tree sums over q.
+//  * bcsr_row_kernel (bs > 32): one thread per scalar row.
+//  * csr_subwarp_kernel: G lanes per row, strided over its entries
+//    (the bs = 1 case and plain CSR).
+//
+// Values are loaded with the streaming (evict-first) hint, x through the
+// read-only path. No tensor cores: a single-vector product has no reuse of A
+// to feed them.
+#include "device_common.cuh"
+#include "internal.h"
+
+#include <algorithm>
+
+namespace bmfp
+{
+namespace
+{
+constexpr int kThreads = 256;
+
+template <typename T, int BS, int G, int U>
+__global__ void __launch_bounds__ (kThreads)
+  bcsr_flat_kernel (int n_block_rows, const int *__restrict__ row_ptr,
+                    const int *__restrict__ cols, const T *__restrict__ vals,
+                    const T *__restrict__ x, T *__restrict__ y)
+{
+  using V16 = dev::Vec16<T>;
+  constexpr int V = V16::N;
+  constexpr int E = BS * BS;
+  constexpr int CH = G * V; // elements one group iteration covers
+  static_assert (E % V == 0, "a block must be a whole number of 16-byte vectors");
+  static_assert (CH >= BS, "a group chunk must cover at least one block line");
+
+  const int64_t tid = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  const int group = (int) (tid / G);
+  const int gl = threadIdx.x & (G - 1);
+  if (group >= n_block_rows)
+    return; // groups are lane-aligned, so a whole group leaves together
+  const unsigned mask = dev::group_mask<G> ();
+
+  const int beg = __ldg (row_ptr + group);
+  const int nblk = __ldg (row_ptr + group + 1) - beg;
+  const T *vb = vals + (size_t) beg * E;
+  const int *cb = cols + beg;
+
+  if constexpr (CH >= E)
+    {
+      constexpr int BPI = CH / E; // whole blocks per group iteration
+      const int bl = (gl * V) / E;
+      const int o = (gl * V) % E;
+      if constexpr (V <= BS)
+        {
+          // V consecutive values of one block line: row o/BS, columns c0..c0+V-1.
+          const int c0 = o % BS;
+          T acc = 0;
+          for (int b0 = 0; b0 < nblk; b0 += BPI * U)
+            {
+              V16 a[U];
+              int c[U];
+#pragma unroll
+              for (int u = 0; u < U; u++)
+                {
+                  const int b = b0 + u * BPI + bl;
+                  c[u] = -1;
+                  if (b < nblk)
+                    {
+                      a[u] = dev::ld_stream16 (vb + b * E + o);
+                      c[u] = __ldg (cb + b);
+                    }
+                }
+#pragma unroll
+              for (int u = 0; u < U; u++)
+                if (c[u] >= 0)
+                  {
+                    const V16 xv = dev::ld_cached16 (x + (size_t) c[u] * BS + c0);
+#pragma unroll
+                    for (int v = 0; v < V; v++)
+                      acc = fma (a[u].v[v], xv.v[v], acc);
+                  }
+            }
+          // Sum over the column-group bits (below BS/V) and the block bits
+          // (E/V and above); the row bits in between stay distinct.
+#pragma unroll
+          for (int off = 1; off < BS / V; off <<= 1)
+            acc += __shfl_xor_sync (mask, acc, off);
+#pragma unroll
+          for (int off = E / V; off < G; off <<= 1)
+            acc += __shfl_xor_sync (mask, acc, off);
+          if (gl < E / V && (gl % (BS / V)) == 0)
+            y[(size_t) group * BS + gl / (BS / V)] = acc;
+        }
+      else
+        {
+          // V > BS only for bs = 2 in float: one vector is a whole block
+          // (a00 a01 a10 a11).
+          static_assert (V == E, "unexpected vector/block shape");
+          T acc0 = 0, acc1 = 0;
+          for (int b0 = 0; b0 < nblk; b0 += BPI * U)
+            {
+              V16 a[U];
+              int c[U];
+#pragma unroll
+              for (int u = 0; u < U; u++)
+                {
+                  const int b = b0 + u * BPI + bl;
+                  c[u] = -1;
+                  if (b < nblk)
+                    {
+                      a[u] = dev::ld_stream16 (vb + b * E);
+                      c[u] = __ldg (cb + b);
+                    }
+                }
+#pragma unroll
+              for (int u = 0; u < U; u++)
+                if (c[u] >= 0)
+                  {
+                    T x0, x1;
+                    dev::ld_cached2 (x + (size_t) c[u] * 2, x0, x1);
+                    acc0 = fma (a[u].v[0], x0, acc0);
+                    acc0 = fma (a[u].v[1], x1, acc0);
+                    acc1 = fma (a[u].v[2], x0, acc1);
+                    acc1 = fma (a[u].v[3], x1, acc1);
+                  }
+            }
+          acc0 = dev::group_sum<G> (acc0);
+          acc1 = dev::group_sum<G> (acc1);
+          if (gl == 0)
+            {
+              y[(size_t) group * 2] = acc0;
+              y[(size_t) group * 2 + 1] = acc1;
+            }
+        }
+    }
+  else
+    {
+      // Large blocks: NP phases per block; in phase p lane l holds row
+      // p*RPP + (l*V)/BS, columns c0..c0+V-1 with c0 = (l*V) % BS.
+      constexpr int NP = E / CH;
+      constexpr int RPP = CH / BS;
+      const int c0 = (gl * V) % BS;
+      const int rl = (gl * V) / BS;
+      T acc[NP];
+#pragma unroll
+      for (int p = 0; p < NP; p++)
+        acc[p] = 0;
+#pragma unroll 2
+      for (int b = 0; b < nblk; b++)
+        {
+          const T *blk = vb + b * E + gl * V;
+          V16 a[NP];
+#pragma unroll
+          for (int p = 0; p < NP; p++)
+            a[p] = dev::ld_stream16 (blk + p * CH);
+          const int c = __ldg (cb + b);
+          const V16 xv = dev::ld_cached16 (x + (size_t) c * BS + c0);
+#pragma unroll
+          for (int p = 0; p < NP; p++)
+#pragma unroll
+            for (int v = 0; v < V; v++)
+              acc[p] = fma (a[p].v[v], xv.v[v], acc[p]);
+        }
+#pragma unroll
+      for (int p = 0; p < NP; p++)
+#pragma unroll
+        for (int off = 1; off < BS / V; off <<= 1)
+          acc[p] += __shfl_xor_sync (mask, acc[p], off);
+      if ((gl % (BS / V)) == 0)
+#pragma unroll
+        for (int p = 0; p < NP; p++)
+          y[(size_t) group * BS + p * RPP + rl] = acc[p];
+    }
+}
+
+// Warp per block row, lane (q, r) = (lane / bs, lane % bs) for q < 32/bs.
+template <typename T, int BSC>
+__global__ void __launch_bounds__ (kThreads)
+  bcsr_tpr_kernel (int n_block_rows, int bs_rt, const int *__restrict__ row_ptr,
+                   const int *__restrict__ cols, const T *__restrict__ vals,
+                   const T *__restrict__ x, T *__restrict__ y)
+{
+  const int bs = BSC ? BSC : bs_rt;
+  const int Q = 32 / bs;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= n_block_rows)
+    return; // whole warp
+  const int q = lane / bs, r = lane % bs;
+  const bool live = q < Q;
+  const int beg = __ldg (row_ptr + warp), end = __ldg (row_ptr + warp + 1);
+  T acc = 0;
+  if (live)
+    for (int b = beg + q; b < end; b += Q)
+      {
+        const T *a = vals + (size_t) b * bs * bs + r * bs;
+        const T *xb = x + (size_t) __ldg (cols + b) * bs;
+        for (int c = 0; c < bs; c++)
+          acc = fma (dev::ld_stream (a + c), dev::ld_cached (xb + c), acc);
+      }
+  int top = 1;
+  while (top < Q)
+    top <<= 1;
+  for (int s = top >> 1; s > 0; s >>= 1)
+    {
+      const T other = __shfl_down_sync (0xffffffffu, acc, s * bs);
+      if (live && q + s < Q)
+        acc += other;
+    }
+  if (q == 0)
+    y[(size_t) warp * bs + r] = acc;
+}
+
+// Thread per scalar row (bs > 32).
+template <typename T>
+__global__ void __launch_bounds__ (kThreads)
+  bcsr_row_kernel (int n_block_rows, int bs, const int *__restrict__ row_ptr,
+                   const int *__restrict__ cols, const T *__restrict__ vals,
+                   const T *__restrict__ x, T *__restrict__ y)
+{
+  const int64_t idx = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t br = idx / bs;
+  const int r = (int) (idx % bs);
+  if (br >= n_block_rows)
+    return;
+  T acc = 0;
+  for (int b = __ldg (row_ptr + br); b < __ldg (row_ptr + br + 1); b++)
+    {
+      const T *a = vals + (size_t) b * bs * bs + (size_t) r * bs;
+      const T *xb = x + (size_t) __ldg (cols + b) * bs;
+      for (int c = 0; c < bs; c++)
+        acc = fma (a[c], dev::ld_cached (xb + c), acc);
+    }
+  y[idx] = acc;
+}
+
+template <typename T, int G>
+__global__ void __launch_bounds__ (kThreads)
+  csr_subwarp_kernel (int n_rows, const int *__restrict__ row_ptr, const int *__restrict__ cols,
+                      const T *__restrict__ vals, const T *__restrict__ x, T *__restrict__ y)
+{
+  const int64_t tid = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t row = tid / G;
+  const int gl = threadIdx.x & (G - 1);
+  if (row >= n_rows)
+    return;
+  const int beg = __ldg (row_ptr + row), end = __ldg (row_ptr + row + 1);
+  T acc0 = 0, acc1 = 0;
+  int e = beg + gl;
+  for (; e + G < end; e += 2 * G)
+    {
+      const T a0 = dev::ld_stream (vals + e), a1 = dev::ld_stream (vals + e + G);
+      const int c0 = __ldg (cols + e), c1 = __ldg (cols + e + G);
+      acc0 = fma (a0, dev::ld_cached (x + c0), acc0);
+      acc1 = fma (a1, dev::ld_cached (x + c1), acc1);
+    }
+  if (e < end)
+    acc0 = fma (dev::ld_stream (vals + e), dev::ld_cached (x + __ldg (cols + e)), acc0);
+  T acc = dev::group_sum<G> (acc0 + acc1);
+  if (gl == 0)
+    y[row] = acc;
+}
+
+// ---------------------------------------------------------------- dispatch
+
+inline int vec_elems (int dtype) { return dtype == BMFP_R64F ? 2 : 4; }
+
+inline bool flat_bs (int bs) { return bs == 2 || bs == 4 || bs == 8 || bs == 16 || bs == 32; }
+
+inline bool flat_lanes_ok (int dtype, int bs, int g)
+{
+  return (g == 2 || g == 4 || g == 8 || g == 16 || g == 32) && g * vec_elems (dtype) >= bs;
+}
+
+template <typename T, int BS, int G>
+int launch_flat_g (int nbr, const int *rp, const int *c, const T *v, const T *x, T *y,
+                   cudaStream_t s)
+{
+  if constexpr (G * dev::Vec16<T>::N < BS)
+    return fail (BMFP_ERROR_INVALID_VALUE, "lane count too small for this block size");
+  else
+    {
+      const int64_t threads = (int64_t) nbr * G;
+      const unsigned grid = (unsigned) ((threads + kThreads - 1) / kThreads);
+      bcsr_flat_kernel<T, BS, G, 4><<<grid, kThreads, 0, s>>> (nbr, rp, c, v, x, y);
+      BMFP_LAUNCH_CHECK ();
+      return BMFP_SUCCESS;
+    }
+}
+
+template <typename T, int BS>
+int launch_flat (int nbr, int g, const int *rp, const int *c, const T *v, const T *x, T *y,
+                 cudaStream_t s)
+{
+  switch (g)
+    {
+    case 2: return launch_flat_g<T, BS, 2> (nbr, rp, c, v, x, y, s);
+    case 4: return launch_flat_g<T, BS, 4> (nbr, rp, c, v, x, y, s);
+    case 8: return launch_flat_g<T, BS, 8> (nbr, rp, c, v, x, y, s);
+    case 16: return launch_flat_g<T, BS, 16> (nbr, rp, c, v, x, y, s);
+    case 32: return launch_flat_g<T, BS, 32> (nbr, rp, c, v, x, y, s);
+    default: return fail (BMFP_ERROR_INVALID_VALUE, "invalid lane count %d", g);
+    }
+}
+
+template <typename T, int G>
+int launch_csr_g (int n, const int *rp, const int *c, const T *v, const T *x, T *y, cudaStream_t s)
+{
+  const int64_t threads = (int64_t) n * G;
+  const unsigned grid = (unsigned) ((threads + kThreads - 1) / kThreads);
+  csr_subwarp_kernel<T, G><<<grid, kThreads, 0, s>>> (n, rp, c, v, x, y);
+  BMFP_LAUNCH_CHECK ();
+  return BMFP_SUCCESS;
+}
+
+template <typename T>
+int launch_csr (int n, int g, const int *rp, const int *c, const T *v, const T *x, T *y,
+                cudaStream_t s)
+{
+  switch (g)
+    {
+    case 1: return launch_csr_g<T, 1> (n, rp, c, v, x, y, s);
+    case 2: return launch_csr_g<T, 2> (n, rp, c, v, x, y, s);
+    case 4: return launch_csr_g<T, 4> (n, rp, c, v, x, y, s);
+    case 8: return launch_csr_g<T, 8> (n, rp, c, v, x, y, s);
+    case 16: return launch_csr_g<T, 16> (n, rp, c, v, x, y, s);
+    case 32: return launch_csr_g<T, 32> (n, rp, c, v, x, y, s);
+    default: return fail (BMFP_ERROR_INVALID_VALUE, "invalid lane count %d", g);
+    }
+}
+
+inline int csr_default_lanes (double avg_nnz_per_row)
+{
+  int g = 1;
+  while (g < 32 && g < avg_nnz_per_row)
+    g <<= 1;
+  return g;
+}
+
+template <typename T>
+int native_bcsr_typed (int nbr, int bs, int64_t nnzb, const int *rp, const int *c, const T *v,
+                       const T *x, T *y, int lanes, cudaStream_t s)
+{
+  const double avg = nbr > 0 ? (double) nnzb / nbr : 0.0;
+  const int dtype = sizeof (T) == 8 ? BMFP_R64F : BMFP_R32F;
+  if (bs == 1)
+    return launch_csr<T> (nbr, lanes ? lanes : csr_default_lanes (avg), rp, c, v, x, y, s);
+  // The flat kernel issues 16-byte vector loads of values and x: it needs
+  // both base pointers 16-byte aligned (cudaMalloc gives 256). Misaligned
+  // views fall through to the scalar-load kernel below.
+  const bool aligned = ((reinterpret_cast<uintptr_t> (v) | reinterpret_cast<uintptr_t> (x)) & 15u) == 0;
+  if (flat_bs (bs) && aligned)
+    {
+      const int g = lanes ? lanes : native_default_lanes (dtype, bs, avg);
+      if (!flat_lanes_ok (dtype, bs, g))
+        return fail (BMFP_ERROR_INVALID_VALUE, "lane count %d not valid for bs=%d", g, bs);
+      switch (bs)
+        {
+        case 2: return launch_flat<T, 2> (nbr, g, rp, c, v, x, y, s);
+        case 4: return launch_flat<T, 4> (nbr, g, rp, c, v, x, y, s);
+        case 8: return launch_flat<T, 8> (nbr, g, rp, c, v, x, y, s);
+        case 16: return launch_flat<T, 16> (nbr, g, rp, c, v, x, y, s);
+        default: return launch_flat<T, 32> (nbr, g, rp, c, v, x, y, s);
+        }
+    }
+  if (bs <= 32)
+    {
+      const int64_t threads = (int64_t) nbr * 32;
+      const unsigned grid = (unsigned) ((threads + kThreads - 1) / kThreads);
+      if (bs == 3)
+        bcsr_tpr_kernel<T, 3><<<grid, kThreads, 0, s>>> (nbr, bs, rp, c, v, x, y);
+      else
+        bcsr_tpr_kernel<T, 0><<<grid, kThreads, 0, s>>> (nbr, bs, rp, c, v, x, y);
+      BMFP_LAUNCH_CHECK ();
+      return BMFP_SUCCESS;
+    }
+  const int64_t threads = (int64_t) nbr * bs;
+  const unsigned grid = (unsigned) ((threads + kThreads - 1) / kThreads);
+  bcsr_row_kernel<T><<<grid, kThreads, 0, s>>> (nbr, bs, rp, c, v, x, y);
+  BMFP_LAUNCH_CHECK ();
+  return BMFP_SUCCESS;
+}
+} // namespace
+
+int native_default_lanes (int dtype, int bs, double avg_blocks_per_row)
+{
+  if (bs == 1)
+    return csr_default_lanes (avg_blocks_per_row);
+  if (!flat_bs (bs))
+    return 32;
+  // Aim for about two 16-byte vectors per lane per block row, within the
+  // lane counts this block size allows.
+  const double vectors = avg_blocks_per_row * bs * bs / vec_elems (dtype);
+  int g = 2;
+  while (g < 32 && 2.0 * g < vectors)
+    g <<= 1;
+  while (!flat_lanes_ok (dtype, bs, g) && g < 32)
+    g <<= 1;
+  return g;
+}
+
+int native_lane_candidates (int dtype, int bs, int *out, int max_out)
+{
+  int n = 0;
+  if (bs == 1)
+    {
+      for (int g = 1; g <= 32 && n < max_out; g <<= 1)
+        out[n++] = g;
+      return n;
+    }
+  if (!flat_bs (bs))
+    return 0;
+  for (int g = 2; g <= 32 && n < max_out; g <<= 1)
+    if (flat_lanes_ok (dtype, bs, g))
+      out[n++] = g;
+  return n;
+}
+
+int spmv_native_bcsr (int dtype, int nbr, int bs, int64_t nnzb, const int *row_ptr,
+                      const int *cols, const void *vals, const void *x, void *y, int lanes,
+                      cudaStream_t stream)
+{
+  if (nbr == 0)
+    return BMFP_SUCCESS;
+  if (dtype == BMFP_R64F)
+    return native_bcsr_typed<double> (nbr, bs, nnzb, row_ptr, cols, (const double *) vals,
+                                      (const double *) x, (double *) y, lanes, stream);
+  return native_bcsr_typed<float> (nbr, bs, nnzb, row_ptr, cols, (const float *) vals,
+                                   (const float *) x, (float *) y, lanes, stream);
+}
+
+int spmv_native_csr (int dtype, int n_rows, int64_t nnz, const int *row_ptr, const int *cols,
+                     const void *vals, const void *x, void *y, int lanes, cudaStream_t stream)
+{
+  if (n_rows == 0)
+    return BMFP_SUCCESS;
+  const int g = lanes ? lanes : csr_default_lanes (n_rows ? (double) nnz / n_rows : 0.0);
+  if (dtype == BMFP_R64F)
+    return launch_csr<double> (n_rows, g, row_ptr, cols, (const double *) vals,
+                               (const double *) x, (double *) y, stream);
+  return launch_csr<float> (n_rows, g, row_ptr, cols, (const float *) vals, (const float *) x,
+                            (float *) y, stream);
+}
+} // namespace bmfp

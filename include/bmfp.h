@@ -1,0 +1,253 @@
+/*
+ * bmfp.h — C ABI of the GB300 (sm_103a) block-sparse library.
+ *
+ * One shared library, libbmfp.so, exports every function below with C
+ * linkage: plain pointers and sizes, no C++ or torch types. The C++ headers
+ * under include/bmfp/ rebuild the reference's own host API
+ * (gpu_csr_spmv / gpu_csr_vector_spmv / gpu_bcsr_spmv, gpu_bicgstab,
+ * bcsr_matrix_class / csr_matrix_class, measurement_class) on top of it.
+ *
+ * Each entry names the reference interface it replaces (paths inside
+ * gevtushenko/block_matrix_format_performance).
+ *
+ * Conventions
+ *  - Every function returns an int status (BMFP_SUCCESS == 0). On failure
+ *    bmfp_last_error() returns a message for the calling thread. Nothing in
+ *    the library prints, exits or resets the device (the reference's
+ *    gpuCheck did both, gpu/bicgstab.cu:12-21).
+ *  - Indices are 32-bit signed (the reference instantiates index_type=int,
+ *    gpu/gpu_matrix_multiplier.cu:1338-1339).
+ *  - BCSR values: nnzb blocks of bs*bs, row-major inside a block
+ *    (common/matrix_converters.h:26), or column-major where a variant says
+ *    so (the transpose_blocks layout, common/matrix_converters.h:32-49).
+ *  - "d_" pointers are device memory, "h_" pointers host memory.
+ *  - stream is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *    Device work is asynchronous on that stream unless a function says
+ *    otherwise.
+ */
+#ifndef BMFP_H
+#define BMFP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define BMFP_API __attribute__ ((visibility ("default")))
+#else
+#define BMFP_API
+#endif
+
+/* ----------------------------------------------------------------- status */
+enum bmfp_status
+{
+  BMFP_SUCCESS = 0,
+  BMFP_ERROR_INVALID_VALUE = 1, /* bad size, pointer, enum or layout */
+  BMFP_ERROR_CUDA = 2,          /* a CUDA runtime / cuSPARSE call failed */
+  BMFP_ERROR_OUT_OF_MEMORY = 3, /* device allocation failed */
+  BMFP_ERROR_NOT_SUPPORTED = 4, /* valid request this build does not serve */
+  BMFP_ERROR_BREAKDOWN = 5,     /* BiCGStab rho, (rh,v) or (t,t) vanished */
+  BMFP_ERROR_NOT_CONVERGED = 6, /* iteration limit reached before tolerance */
+  BMFP_ERROR_TIMEOUT = 7,       /* a bounded device wait gave up */
+  BMFP_ERROR_BUDGET = 8,        /* request does not fit the HBM budget */
+  BMFP_PENDING = 9              /* asynchronous request not finished yet */
+};
+
+enum bmfp_dtype
+{
+  BMFP_R32F = 0, /* float  */
+  BMFP_R64F = 1  /* double */
+};
+
+/* Thread-local message of the last failure on the calling thread. */
+BMFP_API const char *bmfp_last_error (void);
+/* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
+BMFP_API int bmfp_version (void);
+/* Number of CUDA devices visible (0 on a host without a GPU; never fails). */
+BMFP_API int bmfp_device_count (void);
+
+/* ------------------------------------------------------------ SpMV kernels
+ * Variants keep the reference's format strings (the keys of its result.json,
+ * gpu/gpu_matrix_multiplier.cu and main.cpp). Each is a GB300 kernel written
+ * for this library with that variant's thread mapping; BMFP_SPMV_BCSR_NATIVE
+ * and BMFP_SPMV_CSR_NATIVE are the tuned sm_103a kernels.
+ *
+ *  variant                                value layout  reference
+ *  CSR_SCALAR     "GPU CSR"                     CSR     csr_spmv_kernel .cu:65-86
+ *  CSR_VECTOR     "GPU CSR-Vector"              CSR     csr_spmv_vector_kernel .cu:165-196
+ *  CSR_NATIVE     "GPU CSR (GB300 sub-warp)"    CSR     (new)
+ *  BCSR_ROW_THREAD "GPU BCSR (row major, thread per row)"        row  .cu:275-304
+ *  BCSR_ROW_WARP   "GPU BCSR (row major, warp per row)"          row  .cu:306-339
+ *  BCSR_COL_THREAD "GPU BCSR (column major, thread per row)"     col  .cu:341-370
+ *  BCSR_COL_THREAD_TEMPLATE "... thread per row, template)"      col  .cu:372-400
+ *  BCSR_COL_COAL_X "... thread per row, coal x)"                 col  .cu:402-435
+ *  BCSR_COL_COAL_X_TEMPLATE "... coal x, template)"              col  .cu:437-469
+ *  BCSR_COL_BY_COL "GPU BCSR (column major, column-by-column)"   col  .cu:485-528
+ *  BCSR_COL_BY_COL_FASTDIV "... column-by-column, int fastdiv)"  col  .cu:530-576
+ *  BCSR_COL_BY_COL_PO2 "... column-by-column, int po2)"          col  .cu:584-629
+ *  BCSR_COL_BY_COL_TEMPLATE "... column-by-column, template)"    col  .cu:631-673
+ *  BCSR_JIT        "jit" (bs-specialised column-by-column)       col  main.cpp:178-230
+ *  CUSPARSE_ROW    "GPU BSR (cuSPARSE, row major)"               row  .cu:676-734,879
+ *  CUSPARSE_COL    "GPU BSR (cuSPARSE, column major)"            col  .cu:927
+ *  BCSR_NATIVE     "GPU BCSR (GB300 native)"                     row  (new)
+ *
+ * Fixes over the reference, on purpose: the coal-x variants stage the x
+ * segment of every block row they serve (the reference's only read the first
+ * block row's segment, correct only for constant x), and column-by-column
+ * handles block sizes that do not divide 32.
+ */
+enum bmfp_spmv_variant
+{
+  BMFP_SPMV_CSR_SCALAR = 0,
+  BMFP_SPMV_CSR_VECTOR = 1,
+  BMFP_SPMV_CSR_NATIVE = 2,
+  BMFP_SPMV_BCSR_ROW_THREAD = 3,
+  BMFP_SPMV_BCSR_ROW_WARP = 4,
+  BMFP_SPMV_BCSR_COL_THREAD = 5,
+  BMFP_SPMV_BCSR_COL_THREAD_TEMPLATE = 6,
+  BMFP_SPMV_BCSR_COL_COAL_X = 7,
+  BMFP_SPMV_BCSR_COL_COAL_X_TEMPLATE = 8,
+  BMFP_SPMV_BCSR_COL_BY_COL = 9,
+  BMFP_SPMV_BCSR_COL_BY_COL_FASTDIV = 10,
+  BMFP_SPMV_BCSR_COL_BY_COL_PO2 = 11,
+  BMFP_SPMV_BCSR_COL_BY_COL_TEMPLATE = 12,
+  BMFP_SPMV_BCSR_JIT = 13,
+  BMFP_SPMV_CUSPARSE_ROW = 14,
+  BMFP_SPMV_CUSPARSE_COL = 15,
+  BMFP_SPMV_BCSR_NATIVE = 16,
+  BMFP_SPMV_VARIANT_COUNT = 17
+};
+
+/* Reference format string of a variant ("GPU CSR", ...), or NULL. */
+BMFP_API const char *bmfp_spmv_variant_name (int variant);
+/* 1 if the variant reads column-major blocks, 0 row-major/CSR, -1 invalid. */
+BMFP_API int bmfp_spmv_variant_layout (int variant);
+/* 1 if the variant multiplies CSR, 0 BCSR, -1 invalid. */
+BMFP_API int bmfp_spmv_variant_is_csr (int variant);
+
+/* y = A x over device CSR arrays (n_rows+1 row offsets, nnz columns/values).
+ * Replaces the kernels launched by gpu_csr_spmv / gpu_csr_vector_spmv
+ * (gpu/gpu_matrix_multiplier.cu:88-163, 198-273) without their per-call
+ * allocation and copies. variant: CSR_SCALAR, CSR_VECTOR or CSR_NATIVE. */
+BMFP_API int bmfp_csr_spmv (int dtype, int variant, int n_rows, int n_cols, int64_t nnz,
+                            const int *d_row_ptr, const int *d_cols, const void *d_values,
+                            const void *d_x, void *d_y, void *stream);
+
+/* y = A x over device BCSR arrays (n_block_rows+1 offsets, nnzb block
+ * columns, nnzb*bs*bs values in the variant's layout). Replaces the kernel
+ * launches inside gpu_bcsr_spmv (gpu/gpu_matrix_multiplier.cu:736-1331) and
+ * the JIT launch (main.cpp:232-294). */
+BMFP_API int bmfp_bcsr_spmv (int dtype, int variant, int n_block_rows, int n_block_cols, int bs,
+                             int64_t nnzb, const int *d_row_ptr, const int *d_cols,
+                             const void *d_values, const void *d_x, void *d_y, void *stream);
+
+/* Lanes per block row the native kernel would use for this shape (0 = the
+ * built-in heuristic); lets callers and the autotuner pin the choice.
+ * Valid group sizes: 0, 2, 4, 8, 16, 32 (clamped to what the block size
+ * allows). Affects only BMFP_SPMV_BCSR_NATIVE. */
+BMFP_API int bmfp_bcsr_spmv_native_ex (int dtype, int n_block_rows, int bs, int64_t nnzb,
+                                       const int *d_row_ptr, const int *d_cols,
+                                       const void *d_values, const void *d_x, void *d_y,
+                                       int lanes_per_block_row, void *stream);
+BMFP_API int bmfp_bcsr_native_default_lanes (int dtype, int bs, double avg_blocks_per_row);
+
+/* ------------------------------------------------ device matrix handles ---
+ * A device-resident BCSR (or CSR when bs is given as 0 to *_csr) matrix owned
+ * by the library: one upload, then any number of products. The reference
+ * re-allocated and re-uploaded per call (gpu/gpu_matrix_multiplier.cu:106-115,
+ * 757-766). */
+typedef struct bmfp_matrix_s *bmfp_matrix_t;
+
+/* Upload a host BCSR matrix with row-major blocks. dtype is the storage and
+ * arithmetic type on the device. Synchronous with respect to the host
+ * arrays (they may be freed on return). */
+BMFP_API int bmfp_matrix_create_bcsr (bmfp_matrix_t *out, int dtype, int n_block_rows,
+                                      int n_block_cols, int bs, int64_t nnzb,
+                                      const int *h_row_ptr, const int *h_cols,
+                                      const void *h_values, void *stream);
+/* Upload a host CSR matrix. */
+BMFP_API int bmfp_matrix_create_csr (bmfp_matrix_t *out, int dtype, int n_rows, int n_cols,
+                                     int64_t nnz, const int *h_row_ptr, const int *h_cols,
+                                     const void *h_values, void *stream);
+/* Same from arrays already on the device (copied device-to-device). */
+BMFP_API int bmfp_matrix_create_bcsr_device (bmfp_matrix_t *out, int dtype, int n_block_rows,
+                                             int n_block_cols, int bs, int64_t nnzb,
+                                             const int *d_row_ptr, const int *d_cols,
+                                             const void *d_values, void *stream);
+/* A copy of a matrix converted to another value type on the device
+ * (e.g. the FP32 shadow of an FP64 operator for mixed precision). */
+BMFP_API int bmfp_matrix_convert (bmfp_matrix_t *out, bmfp_matrix_t src, int dtype, void *stream);
+BMFP_API int bmfp_matrix_destroy (bmfp_matrix_t m);
+/* Shape query: any output pointer may be NULL. bs = 0 for CSR. */
+BMFP_API int bmfp_matrix_info (bmfp_matrix_t m, int *dtype, int *n_rows, int *n_cols, int *bs,
+                               int64_t *nnz_blocks, int64_t *bytes_per_spmv);
+/* Device pointers of the stored arrays (values in row-major blocks). */
+BMFP_API int bmfp_matrix_device_arrays (bmfp_matrix_t m, const int **d_row_ptr,
+                                        const int **d_cols, const void **d_values);
+/* y = A x with the tuned kernel (native BCSR or native CSR). x and y are
+ * device vectors of the matrix dtype, n_cols*bs and n_rows*bs long. */
+BMFP_API int bmfp_matrix_spmv (bmfp_matrix_t m, const void *d_x, void *d_y, void *stream);
+/* Time candidate lane counts on this matrix (CUDA events, synchronises the
+ * stream) and keep the fastest for later bmfp_matrix_spmv calls. x and y are
+ * scratch device vectors of the right size. Optional: the default choice is
+ * the built-in heuristic. */
+BMFP_API int bmfp_matrix_autotune (bmfp_matrix_t m, const void *d_x, void *d_y, void *stream,
+                                   int *chosen_lanes);
+
+/* --------------------------------------------------- host-side utilities ---
+ * Pure host functions (no GPU needed). */
+
+/* BCSR -> CSR, common/matrix_converters.h:88-117. Output sizes
+ * n_block_rows*bs+1, nnzb*bs*bs, nnzb*bs*bs. */
+BMFP_API int bmfp_bcsr_to_csr (int dtype, int n_block_rows, int bs, const int *brow_ptr,
+                               const int *bcols, const void *bvals, int *row_ptr, int *cols,
+                               void *vals);
+/* CSR -> BCSR (new; the inverse of bmfp_bcsr_to_csr, bit-exact on its
+ * output). Pass 1: bvals == NULL and bcols == NULL fills brow_ptr
+ * (n_rows/bs+1) and *nnzb. Pass 2: fills bcols (sorted) and row-major block
+ * values, zero where the CSR holds no entry. */
+BMFP_API int bmfp_csr_to_bcsr (int dtype, int n_rows, int n_cols, int bs, const int *row_ptr,
+                               const int *cols, const void *vals, int *brow_ptr, int64_t *nnzb,
+                               int *bcols, void *bvals);
+/* Row-major -> column-major blocks, common/matrix_converters.h:32-49.
+ * (Applied twice it is the identity.) */
+BMFP_API int bmfp_transpose_blocks (int dtype, int n_block_rows, int bs, const int *row_ptr,
+                                    const void *vals, void *out);
+/* The reference's contiguous-band generator, common/matrix_converters.h:157-196:
+ * sizes n_rows+1, n_rows*blocks_per_row, n_rows*blocks_per_row*bs*bs. */
+BMFP_API int bmfp_gen_n_diag_bcsr (int dtype, int n_rows, int blocks_per_row, int bs,
+                                   int *row_ptr, int *cols, void *vals);
+/* Seeded random-band BCSR (new): block row i holds min(k, W) distinct block
+ * columns drawn from [max(0,i-h), min(nbr-1,i+h)] (W wide), sorted, values
+ * uniform in [-1,1). Per-row SplitMix64 streams: the output depends only on
+ * (seed, shape). Pass 1 (cols == NULL, vals == NULL): row_ptr and *nnzb.
+ * Pass 2: cols and vals. */
+BMFP_API int bmfp_gen_band_bcsr (int dtype, int n_block_rows, int blocks_per_row, int half_band,
+                                 int bs, uint64_t seed, int *row_ptr, int64_t *nnzb, int *cols,
+                                 void *vals);
+/* x_i uniform in [-1,1) from SplitMix64 of (seed, stream, i). */
+BMFP_API int bmfp_gen_uniform_vector (int dtype, int64_t n, uint64_t seed, uint64_t stream,
+                                      void *out);
+/* Q4 plane-stress elasticity (new): nx*ny node grid of unit squares, E, nu,
+ * thickness 1; node (i,j) -> block row j*nx+i with DOFs (ux,uy); left column
+ * clamped (unit diagonal, zero rows/columns kept in the pattern); BCSR bs=2
+ * with the full 9-node stencil. Pass 1 (cols == NULL): row_ptr, *nnzb.
+ * Pass 2: cols, vals (float64 or float32) and, if rhs != NULL, the load
+ * f_y = -1 on the right column (2*nx*ny entries). */
+BMFP_API int bmfp_gen_q4_elasticity (int dtype, int nx, int ny, double young, double poisson,
+                                     int *row_ptr, int64_t *nnzb, int *cols, void *vals,
+                                     void *rhs);
+/* Algorithmic bytes of one BCSR SpMV: values + block columns + row offsets +
+ * x read once + y written once (value and vector size from dtype). */
+BMFP_API int64_t bmfp_bcsr_spmv_bytes (int dtype, int n_block_rows, int n_block_cols, int bs,
+                                       int64_t nnzb);
+BMFP_API int64_t bmfp_csr_spmv_bytes (int dtype, int n_rows, int n_cols, int64_t nnz);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BMFP_H */
