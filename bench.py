@@ -59,7 +59,7 @@ FALLBACK_HBM_GBS = 6800.0
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--e2e-steps", type=int, default=3)
@@ -67,6 +67,8 @@ def parse_args():
     ap.add_argument("--no-csr-compare", action="store_true")
     ap.add_argument("--sizes", default=",".join(map(str, BLOCK_SIZES)))
     ap.add_argument("--dtypes", default=",".join(DTYPES))
+    ap.add_argument("--n-block-rows", type=int, default=NBR,
+                    help="block rows per matrix (smaller only for profiling captures)")
     return ap.parse_args()
 
 
@@ -146,14 +148,14 @@ class ClockSampler:
 
 # ---------------------------------------------------------------- workload
 
-def build_cases(bm, sizes, dtypes, with_csr):
+def build_cases(bm, sizes, dtypes, nbr):
     cases = []
     for tag in dtypes:
         for bs in sizes:
-            rp, c, v = bm.gen_band_bcsr(NBR, BPR, HALF_BAND, bs, SEED, np_dt(tag))
-            x = bm.gen_uniform_vector(NBR * bs, SEED, X_STREAM, np_dt(tag))
+            rp, c, v = bm.gen_band_bcsr(nbr, BPR, HALF_BAND, bs, SEED, np_dt(tag))
+            x = bm.gen_uniform_vector(nbr * bs, SEED, X_STREAM, np_dt(tag))
             case = {"bs": bs, "tag": tag, "rp": rp, "c": c, "v": v, "x": x, "nnzb": int(c.size),
-                    "bytes": case_bytes(bs, tag, int(c.size))}
+                    "bytes": case_bytes(bs, tag, int(c.size), nbr)}
             cases.append(case)
     return cases
 
@@ -201,7 +203,8 @@ def run_ours(args):
     sizes = [int(s) for s in args.sizes.split(",")]
     dtypes = args.dtypes.split(",")
     t0 = time.time()
-    cases = build_cases(bm, sizes, dtypes, not args.no_csr_compare)
+    nbr = args.n_block_rows
+    cases = build_cases(bm, sizes, dtypes, nbr)
     gen_s = time.time() - t0
 
     stream = torch.cuda.current_stream()
@@ -272,7 +275,7 @@ def run_ours(args):
         for cs in cases:
             crp, cc, cv = bm.bcsr_to_csr(cs["rp"], cs["c"], cs["v"], cs["bs"])
             d_rp, d_c, d_v = (torch.from_numpy(a).cuda() for a in (crp, cc, cv))
-            cbytes = bm.csr_spmv_bytes(np_dt(cs["tag"]), NBR * cs["bs"], NBR * cs["bs"], cc.size)
+            cbytes = bm.csr_spmv_bytes(np_dt(cs["tag"]), nbr * cs["bs"], nbr * cs["bs"], cc.size)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             reps, tot = 5, 0.0
             for r in range(reps + 1):
@@ -311,14 +314,16 @@ def run_ours(args):
             torch.cuda.synchronize()
             m.close()
 
-    e2e_step()
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    e0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
+    e2e_s = float("nan")
+    if args.e2e_steps > 0:
         e2e_step()
-    e2e_s = (time.perf_counter() - e0) / args.e2e_steps
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        e2e_s = (time.perf_counter() - e0) / args.e2e_steps
     if dist:
         t = torch.tensor([e2e_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -327,7 +332,7 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(cases)
+        cpu = cpu_baseline(cases, nbr=nbr)
 
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world,
@@ -335,7 +340,7 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "+".join(dtypes), "data": "synthetic (seeded generator; the reference has no dataset)",
         "config": {
-            "workload": WORKLOAD, "n_block_rows": NBR, "blocks_per_row": BPR, "half_band": HALF_BAND,
+            "workload": WORKLOAD if nbr == NBR else WORKLOAD.replace("100000", str(nbr)), "n_block_rows": nbr, "blocks_per_row": BPR, "half_band": HALF_BAND,
             "block_sizes": sizes, "seed": SEED, "parallelism": f"replicas x{world} (no collective)",
             "l2": "flushed before every product (256 MB write + 512 MB read), outside the timed events",
             "kernel": "GPU BCSR (GB300 native)", "per_case": per_case, "csr_warp_per_row": csr_cmp,
@@ -369,7 +374,7 @@ def cpu_sample(bm, cs, rows):
     return crp, cc, cv, case_bytes(bs, cs["tag"], nnzb, rows)
 
 
-def cpu_baseline(cases, rows=20_000, reps=3):
+def cpu_baseline(cases, rows=20_000, reps=3, nbr=NBR):
     """Oracle restatement of main.cpp:36-45 (one thread) on a bounded sample."""
     import block_matrix_format_performance_gb300 as bm
     from oracle import oracle as orc
@@ -384,7 +389,7 @@ def cpu_baseline(cases, rows=20_000, reps=3):
         tot_s += (time.perf_counter() - t0) / reps
         tot_b += b
     return {"value": round(tot_b / tot_s / 1e9, 2), "unit": "GB/s", "cores": 1, "kind": "port",
-            "sample": f"first {rows} of {NBR} block rows of each of the {len(cases)} sweep matrices, CSR, "
+            "sample": f"first {rows} of {nbr} block rows of each of the {len(cases)} sweep matrices, CSR, "
                       f"{reps} passes; the reference CPU loop main.cpp:36-45 restated in C (-O2)"}
 
 
