@@ -69,6 +69,13 @@ def parse_args():
     ap.add_argument("--dtypes", default=",".join(DTYPES))
     ap.add_argument("--n-block-rows", type=int, default=NBR,
                     help="block rows per matrix (smaller only for profiling captures)")
+    ap.add_argument("--workload", choices=("spmv", "solve"), default="spmv",
+                    help="spmv: the block-size sweep line (default); solve: one Q4 elasticity solve")
+    ap.add_argument("--grid", default="200x50", help="solve: nodes nx x ny of the Q4 grid")
+    ap.add_argument("--precision", default="fp64", choices=("fp64", "fp32", "mixed"))
+    ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--max-iters", type=int, default=200000)
+    ap.add_argument("--repeats", type=int, default=3)
     return ap.parse_args()
 
 
@@ -212,6 +219,8 @@ def run_ours(args):
         cs["m"] = bm.Matrix.from_bcsr(cs["rp"], cs["c"], cs["v"], cs["bs"])
         cs["dx"] = torch.from_numpy(cs["x"]).cuda()
         cs["dy"] = torch.empty_like(cs["dx"])
+        # the library's autotuner times every valid lane count on this matrix
+        cs["lanes"] = cs["m"].autotune(cs["dx"], cs["dy"])
     flush_w = torch.empty(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB
     flush_r = torch.ones(128 << 20, dtype=torch.float32, device="cuda")  # 512 MB
 
@@ -260,7 +269,8 @@ def run_ours(args):
     for i, cs in enumerate(cases):
         ms = per_case_ms[i] / args.steps
         per_case[f"bs{cs['bs']}_{cs['tag']}"] = {"gbs": round(cs["bytes"] / (ms * 1e-3) / 1e9, 1),
-                                                  "us": round(ms * 1e3, 2), "mb": round(cs["bytes"] / 1e6, 1)}
+                                                  "us": round(ms * 1e3, 2), "mb": round(cs["bytes"] / 1e6, 1),
+                                                  "lanes": cs["lanes"]}
     dom = max(range(n), key=lambda i: per_case_ms[i])
     dcs = cases[dom]
     dom_ms = per_case_ms[dom] / args.steps
@@ -441,8 +451,43 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_solve(args):
+    """One Q4 plane-stress solve (the FEM workloads), timed end to end on the
+    device: solves/s, iterations, true residual and bytes per iteration."""
+    import torch
+
+    import block_matrix_format_performance_gb300 as bm
+    from block_matrix_format_performance_gb300 import build as B
+    B.build()
+    nx, ny = (int(t) for t in args.grid.lower().split("x"))
+    rp, c, v, rhs = bm.gen_q4_elasticity(nx, ny)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    s = bm.Solver(A, args.precision, tol=args.tol, max_iters=args.max_iters)
+    d_b = torch.from_numpy(rhs).cuda()
+    d_x = torch.empty_like(d_b)
+    infos = []
+    for _ in range(max(1, args.repeats)):
+        infos.append(s.solve(d_b, d_x))
+    best = min(infos, key=lambda i: i["seconds"])
+    n = 2 * nx * ny
+    spmv_b = bm.bcsr_spmv_bytes(np.float64 if args.precision == "fp64" else np.float32, nx * ny, nx * ny, 2,
+                                int(c.size))
+    per_iter = 2 * spmv_b + 17 * n * (8 if args.precision == "fp64" else 4)
+    it = max(best["iterations"], 1)
+    print(json.dumps({"workload": "solve", "grid": [nx, ny], "dofs": n, "nnzb": int(c.size),
+                      "precision": args.precision, "tol": args.tol, "solves_per_s": round(1.0 / best["seconds"], 3),
+                      "seconds": round(best["seconds"], 4), "us_per_iteration": round(best["seconds"] / it * 1e6, 2),
+                      "bytes_per_iteration": int(per_iter),
+                      "gbs_per_iteration": round(per_iter / (best["seconds"] / it) / 1e9, 1), **best}), flush=True)
+    s.close()
+    A.close()
+
+
 def main():
     args = parse_args()
+    if args.workload == "solve":
+        run_solve(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

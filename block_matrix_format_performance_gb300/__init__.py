@@ -13,7 +13,7 @@ import ctypes
 
 import numpy as np
 
-from ._capi import BmfpError, check, load, LIB_PATH  # noqa: F401
+from ._capi import BmfpError, SolveInfo, SolverOptions, check, load, LIB_PATH  # noqa: F401
 
 R32F, R64F = 0, 1
 
@@ -277,6 +277,64 @@ class Matrix:
     def close(self):
         if self.handle:
             load().bmfp_matrix_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+SOLVE_FP64, SOLVE_FP32, SOLVE_MIXED = 0, 1, 2
+PRECOND_NONE, PRECOND_JACOBI = 0, 1
+_PRECISIONS = {"fp64": SOLVE_FP64, "fp32": SOLVE_FP32, "mixed": SOLVE_MIXED}
+
+
+def solver_options(**kw) -> SolverOptions:
+    """bmfp_solver_options with the library defaults, then keyword overrides."""
+    o = SolverOptions()
+    load().bmfp_solver_options_init(ctypes.byref(o))
+    for k, v in kw.items():
+        if k == "precision" and isinstance(v, str):
+            v = _PRECISIONS[v]
+        if k == "preconditioner" and isinstance(v, str):
+            v = {"none": PRECOND_NONE, "jacobi": PRECOND_JACOBI}[v]
+        setattr(o, k, int(v) if isinstance(v, bool) else v)
+    return o
+
+
+class Solver:
+    """bmfp_solver_t: BiCGStab bound to a device matrix handle."""
+
+    def __init__(self, matrix: "Matrix", precision="fp64", tol=1e-10, max_iters=100000, stream=None, **kw):
+        self.matrix = matrix
+        self.options = solver_options(precision=precision, tolerance=tol, max_iterations=max_iters, **kw)
+        h = ctypes.c_void_p()
+        check(load().bmfp_solver_create(ctypes.byref(h), matrix.handle, ctypes.byref(self.options),
+                                        _stream(stream)))
+        self.handle = h
+
+    def solve(self, d_b, d_x, stream=None, raise_on_failure=False) -> dict:
+        """Solve A x = b for device vectors; returns bmfp_solve_info as a dict."""
+        info = SolveInfo()
+        st = load().bmfp_solver_solve(self.handle, _p(d_b), _p(d_x), ctypes.byref(info), _stream(stream))
+        if st not in (SUCCESS, ERROR_NOT_CONVERGED, ERROR_BREAKDOWN) or (raise_on_failure and st != SUCCESS):
+            check(st)
+        return info.as_dict()
+
+    def solve_host(self, b, stream=None):
+        """Host numpy right-hand side in, host solution and info out."""
+        import torch
+        tdt = torch.float64 if self.matrix.dtype == R64F else torch.float32
+        d_b = torch.from_numpy(np.ascontiguousarray(b, dtype=np_dtype(self.matrix.dtype))).cuda()
+        d_x = torch.empty_like(d_b, dtype=tdt)
+        info = self.solve(d_b, d_x, stream)
+        return d_x.cpu().numpy(), info
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().bmfp_solver_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

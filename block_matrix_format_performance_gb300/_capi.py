@@ -58,8 +58,30 @@ SIGNATURES = {
     "bmfp_gen_q4_elasticity": (c_int, [c_int, c_int, c_int, c_double, c_double, c_void_p, P(c_int64),
                                        c_void_p, c_void_p, c_void_p]),
     "bmfp_bcsr_spmv_bytes": (c_int64, [c_int, c_int, c_int, c_int, c_int64]),
+    "bmfp_solver_options_init": (None, [c_void_p]),
+    "bmfp_solver_create": (c_int, [P(c_void_p), c_void_p, c_void_p, c_void_p]),
+    "bmfp_solver_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "bmfp_solver_destroy": (c_int, [c_void_p]),
     "bmfp_csr_spmv_bytes": (c_int64, [c_int, c_int, c_int, c_int64]),
 }
+
+
+class SolverOptions(ctypes.Structure):
+    """struct bmfp_solver_options (include/bmfp.h)."""
+    _fields_ = [("precision", c_int), ("preconditioner", c_int), ("tolerance", c_double),
+                ("max_iterations", c_int), ("check_true_residual", c_int), ("inner_tolerance", c_double),
+                ("inner_max_iterations", c_int), ("max_refinements", c_int), ("fallback_fp64", c_int),
+                ("iterations_per_graph", c_int)]
+
+
+class SolveInfo(ctypes.Structure):
+    """struct bmfp_solve_info (include/bmfp.h)."""
+    _fields_ = [("status", c_int), ("iterations", c_int), ("iterations_fp32", c_int), ("refinements", c_int),
+                ("restarts", c_int), ("used_fp64_fallback", c_int), ("true_rel_residual", c_double),
+                ("recursive_rel_residual", c_double), ("seconds", c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class BmfpError(RuntimeError):

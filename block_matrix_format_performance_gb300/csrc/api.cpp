@@ -33,25 +33,9 @@ int cuda_fail (cudaError_t e, const char *what, const char *file, int line)
   const int status = e == cudaErrorMemoryAllocation ? BMFP_ERROR_OUT_OF_MEMORY : BMFP_ERROR_CUDA;
   return fail (status, "%s failed: %s (%s:%d)", what, cudaGetErrorString (e), file, line);
 }
-
-int convert_values (int src_dtype, int dst_dtype, int64_t n, const void *src, void *dst,
-                    cudaStream_t stream);
 } // namespace bmfp
 
 using namespace bmfp;
-
-struct bmfp_matrix_s
-{
-  int dtype = BMFP_R64F;
-  int n_rows = 0; // block rows for BCSR, rows for CSR
-  int n_cols = 0; // block columns for BCSR, columns for CSR
-  int bs = 0;     // 0 = CSR
-  int64_t nnz = 0; // blocks for BCSR, entries for CSR
-  int *d_row_ptr = nullptr;
-  int *d_cols = nullptr;
-  void *d_vals = nullptr;
-  int lanes = 0; // tuned lane count, 0 = heuristic
-};
 
 extern "C" {
 

@@ -1,0 +1,804 @@
+// BiCGStab on the GPU: the recurrences of the reference solver
+// (gpu/bicgstab.cu:387-513, optional point-Jacobi right preconditioning as in
+// :201-238), restructured for GB300.
+//
+// One iteration is five phase kernels over all rows, each a fixed persistent
+// grid; the scalars rho, alpha, omega live in device memory (DevState), so no
+// host round trip separates the phases (the reference did four blocking
+// copies and a print per iteration, gpu/bicgstab.cu:447-510):
+//
+//   phase 1  rho = (rh, r), rr = (r, r)    from phase 5's partials
+//            convergence / breakdown test; beta = (rho/rho_prev)(alpha/omega)
+//            p = r + beta (p - omega v);   q = P p
+//   phase 2  v = A q, partial (rh, v)       fused into the SpMV epilogue
+//   phase 3  alpha = rho / (rh, v);         s = r - alpha v;  z = P s
+//   phase 4  t = A z, partials (t, s), (t, t)
+//   phase 5  omega = (t, s) / (t, t);       x += alpha q + omega z;  r = s - omega t
+//            partials (rh, r), (r, r)
+//
+// Algorithmic traffic per iteration: 2 SpMV + 17 n vector elements (no
+// preconditioner). Dot products are per-CTA partial sums written by one phase
+// and summed in a fixed order by every CTA of the next, so every CTA derives
+// bitwise the same scalar and a solve is deterministic for a given grid.
+// The host launches CUDA graphs of `chunk` iterations and only polls the
+// done flag between graphs; phases after convergence return immediately.
+//
+// Differences from the reference, on purpose: the solution returned is the
+// last iterate (the reference copied buffer half 0, bicgstab.cu:515), and a
+// solve finishes with a true-residual check b - A x (restarting from the true
+// residual when the recursive one has drifted below the tolerance first).
+#include "solver.h"
+#include "spmv_core.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+namespace bmfp
+{
+namespace
+{
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+
+enum PartKind
+{
+  kRhR = 0,
+  kRR = 1,
+  kRhV = 2,
+  kTS = 3,
+  kTT = 4,
+  kResRR = 5,
+  kResBB = 6,
+  kParts = 7
+};
+
+template <typename T> struct Args
+{
+  int nbr, bs;
+  const int *rp, *cols;
+  const T *vals;
+  int64_t n;
+  T *x, *r, *rh, *p, *v, *q, *s, *z, *t;
+  const T *P;
+  double *part;
+  int grid;
+  DevState *st;
+};
+
+__device__ __forceinline__ double warp_sum (double v)
+{
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+    v += __shfl_xor_sync (0xffffffffu, v, off);
+  return v;
+}
+
+__device__ __forceinline__ bool is_done (const DevState *st)
+{
+  // Written by an earlier kernel, or by block 0 of this one in a case where
+  // every block takes the same early return anyway.
+  return *reinterpret_cast<const volatile int *> (&st->done) != 0;
+}
+
+// Sum the grid partials of NK kinds in a fixed order (warp 0), broadcast.
+template <int NK>
+__device__ __forceinline__ void sum_parts (const double *part, int grid, const int (&ks)[NK],
+                                           double (&out)[NK])
+{
+  __shared__ double sh[NK];
+  if (threadIdx.x < 32)
+    {
+#pragma unroll
+      for (int k = 0; k < NK; k++)
+        {
+          double acc = 0.0;
+          for (int i = threadIdx.x; i < grid; i += 32)
+            acc += part[ks[k] * grid + i];
+          acc = warp_sum (acc);
+          if (threadIdx.x == 0)
+            sh[k] = acc;
+        }
+    }
+  __syncthreads ();
+#pragma unroll
+  for (int k = 0; k < NK; k++)
+    out[k] = sh[k];
+}
+
+// Reduce per-thread values over the CTA (fixed order) into part[k][blockIdx].
+template <int NK>
+__device__ __forceinline__ void store_parts (double (&v)[NK], double *part, int grid,
+                                             const int (&ks)[NK])
+{
+  __shared__ double sh[NK][kWarps];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NK; k++)
+    {
+      const double s = warp_sum (v[k]);
+      if (lane == 0)
+        sh[k][w] = s;
+    }
+  __syncthreads ();
+  if (threadIdx.x < 32)
+#pragma unroll
+    for (int k = 0; k < NK; k++)
+      {
+        double a = lane < kWarps ? sh[k][lane] : 0.0;
+        a = warp_sum (a);
+        if (lane == 0)
+          part[ks[k] * grid + blockIdx.x] = a;
+      }
+}
+
+#define GRID_STRIDE(i, n)                                                                          \
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < (n);                       \
+       i += (int64_t) gridDim.x * blockDim.x)
+
+// ------------------------------------------------------------ SpMV phases
+
+template <typename T, int BS, int G> struct FlatOp
+{
+  template <class Epi>
+  __device__ static void run (const Args<T> &a, const T *x, T *y, Epi &e)
+  {
+    const int64_t group = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const int64_t ng = (int64_t) gridDim.x * blockDim.x / G;
+    for (int64_t row = group; row < a.nbr; row += ng)
+      core::flat_row<T, BS, G, 4> ((int) row, a.rp, a.cols, a.vals, x, y, e);
+  }
+};
+
+template <typename T, int BSC> struct TprOp
+{
+  template <class Epi>
+  __device__ static void run (const Args<T> &a, const T *x, T *y, Epi &e)
+  {
+    const int64_t warp = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = (int64_t) gridDim.x * blockDim.x >> 5;
+    for (int64_t row = warp; row < a.nbr; row += nw)
+      core::tpr_row<T, BSC> ((int) row, a.bs, a.rp, a.cols, a.vals, x, y, e);
+  }
+};
+
+template <typename T, int G> struct CsrOp
+{
+  template <class Epi>
+  __device__ static void run (const Args<T> &a, const T *x, T *y, Epi &e)
+  {
+    const int64_t group = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const int64_t ng = (int64_t) gridDim.x * blockDim.x / G;
+    for (int64_t row = group; row < a.nbr; row += ng)
+      core::csr_row<T, G> ((int) row, a.rp, a.cols, a.vals, x, y, e);
+  }
+};
+
+template <typename T> struct EpiDot
+{
+  const T *a;
+  double acc = 0.0;
+  __device__ void operator() (int64_t i, T y) { acc = fma ((double) a[i], (double) y, acc); }
+};
+
+template <typename T> struct EpiTS
+{
+  const T *s;
+  double ts = 0.0, tt = 0.0;
+  __device__ void operator() (int64_t i, T t)
+  {
+    ts = fma ((double) s[i], (double) t, ts);
+    tt = fma ((double) t, (double) t, tt);
+  }
+};
+
+template <typename T> struct EpiResidual
+{
+  const T *b;
+  T *r;
+  double rr = 0.0, bb = 0.0;
+  __device__ void operator() (int64_t i, T y)
+  {
+    const T bi = b[i];
+    const T ri = bi - y;
+    r[i] = ri;
+    rr = fma ((double) ri, (double) ri, rr);
+    bb = fma ((double) bi, (double) bi, bb);
+  }
+};
+
+// phase 2: v = A q, partial (rh, v)
+template <typename T, class Op>
+__global__ void __launch_bounds__ (kThreads) phase_v (Args<T> a)
+{
+  if (is_done (a.st))
+    return;
+  EpiDot<T> e{ a.rh };
+  Op::run (a, a.q, a.v, e);
+  double vals[1] = { e.acc };
+  const int ks[1] = { kRhV };
+  store_parts<1> (vals, a.part, a.grid, ks);
+}
+
+// phase 4: t = A z, partials (t, s), (t, t)
+template <typename T, class Op>
+__global__ void __launch_bounds__ (kThreads) phase_t (Args<T> a)
+{
+  if (is_done (a.st))
+    return;
+  EpiTS<T> e{ a.s };
+  Op::run (a, a.z, a.t, e);
+  double vals[2] = { e.ts, e.tt };
+  const int ks[2] = { kTS, kTT };
+  store_parts<2> (vals, a.part, a.grid, ks);
+}
+
+// r = b - A x (x given), partials ||r||^2, ||b||^2 — the true residual.
+template <typename T, class Op>
+__global__ void __launch_bounds__ (kThreads)
+  residual_kernel (Args<T> a, const T *x, const T *b, T *r, T *y)
+{
+  EpiResidual<T> e{ b, r };
+  Op::run (a, x, y, e);
+  double vals[2] = { e.rr, e.bb };
+  const int ks[2] = { kResRR, kResBB };
+  store_parts<2> (vals, a.part, a.grid, ks);
+}
+
+// ------------------------------------------------------------ vector phases
+
+// Fresh start (ZERO: x = 0, r = b) or restart from a given true residual.
+template <typename T, bool ZERO>
+__global__ void __launch_bounds__ (kThreads)
+  start_kernel (Args<T> a, const T *src, double tol, int max_iter, double norm_b)
+{
+  double rr = 0.0;
+  GRID_STRIDE (i, a.n)
+  {
+    const T ri = src[i];
+    if (ZERO)
+      a.x[i] = 0;
+    a.r[i] = ri;
+    a.rh[i] = ri;
+    a.p[i] = 0;
+    a.v[i] = 0;
+    rr = fma ((double) ri, (double) ri, rr);
+  }
+  double vals[2] = { rr, rr };
+  const int ks[2] = { kRhR, kRR };
+  store_parts<2> (vals, a.part, a.grid, ks);
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    {
+      DevState *st = a.st;
+      st->rho_prev = 1.0; // gpu/bicgstab.cu:414-420
+      st->alpha = 1.0;
+      st->omega = 1.0;
+      st->rho = 0.0;
+      st->tol = tol;
+      st->max_iter = max_iter;
+      st->done = 0;
+      st->status = kStateRunning;
+      if (ZERO)
+        {
+          st->iter = 0;
+          st->norm_b = -1.0; // set from the first phase-1 sum
+        }
+      else if (norm_b > 0.0)
+        st->norm_b = norm_b;
+    }
+}
+
+// phase 1
+// GB300's FP64 pipe is narrow (about 1/58 of FP32), so the scalar divides and
+// square roots run once per CTA (thread 0) and reach the other threads
+// through shared memory instead of being evaluated by every thread.
+template <typename T, bool PRE>
+__global__ void __launch_bounds__ (kThreads) phase_p (Args<T> a)
+{
+  DevState *st = a.st;
+  if (is_done (st))
+    return;
+  double s[2];
+  const int ks[2] = { kRhR, kRR };
+  sum_parts<2> (a.part, a.grid, ks, s);
+  __shared__ double sh_beta, sh_omega;
+  __shared__ int sh_status;
+  if (threadIdx.x == 0)
+    {
+      const double rho = s[0], rr = s[1];
+      const double nb_state = st->norm_b;
+      const double nb = nb_state < 0.0 ? sqrt (rr) : nb_state;
+      const double omega = st->omega;
+      int status = kStateRunning;
+      double beta = 0.0;
+      if (nb == 0.0 || sqrt (rr) < st->tol * nb) // gpu/bicgstab.cu:512
+        status = kStateConverged;
+      else if (st->iter >= st->max_iter)
+        status = kStateMaxIter;
+      else if (rho == 0.0 || omega == 0.0 || !isfinite (rho))
+        status = kStateBreakdown;
+      else
+        {
+          beta = rho / st->rho_prev * st->alpha / omega; // gpu/bicgstab.cu:451
+          if (!isfinite (beta))
+            status = kStateBreakdown;
+        }
+      if (blockIdx.x == 0)
+        {
+          st->rr = rr;
+          if (status != kStateRunning)
+            {
+              st->status = status;
+              *reinterpret_cast<volatile int *> (&st->done) = 1;
+            }
+          else
+            st->rho = rho;
+        }
+      sh_beta = beta;
+      sh_omega = omega;
+      sh_status = status;
+    }
+  __syncthreads ();
+  if (sh_status != kStateRunning)
+    return;
+  const T tb = (T) sh_beta, tw = (T) sh_omega;
+  GRID_STRIDE (i, a.n)
+  {
+    const T pn = a.r[i] + tb * (a.p[i] - tw * a.v[i]); // :286-304
+    a.p[i] = pn;
+    if (PRE)
+      a.q[i] = a.P[i] * pn; // :227-238
+  }
+}
+
+// phase 3
+template <typename T, bool PRE>
+__global__ void __launch_bounds__ (kThreads) phase_s (Args<T> a)
+{
+  DevState *st = a.st;
+  if (is_done (st))
+    return;
+  double s[1];
+  const int ks[1] = { kRhV };
+  sum_parts<1> (a.part, a.grid, ks, s);
+  __shared__ double sh_alpha;
+  if (threadIdx.x == 0)
+    {
+      const double alpha = st->rho / s[0]; // gpu/bicgstab.cu:466
+      const bool ok = s[0] != 0.0 && isfinite (alpha);
+      sh_alpha = ok ? alpha : NAN;
+      if (blockIdx.x == 0)
+        {
+          if (ok)
+            {
+              st->alpha = alpha;
+              if (st->norm_b < 0.0)
+                st->norm_b = sqrt (st->rr);
+            }
+          else
+            {
+              st->status = kStateBreakdown;
+              *reinterpret_cast<volatile int *> (&st->done) = 1;
+            }
+        }
+    }
+  __syncthreads ();
+  const double alpha = sh_alpha;
+  if (!isfinite (alpha))
+    return;
+  const T ta = (T) alpha;
+  GRID_STRIDE (i, a.n)
+  {
+    const T si = a.r[i] - ta * a.v[i]; // :306-327
+    a.s[i] = si;
+    if (PRE)
+      a.z[i] = a.P[i] * si;
+  }
+}
+
+// phase 5
+template <typename T, bool PRE>
+__global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
+{
+  DevState *st = a.st;
+  if (is_done (st))
+    return;
+  double s[2];
+  const int ks[2] = { kTS, kTT };
+  sum_parts<2> (a.part, a.grid, ks, s);
+  __shared__ double sh_alpha, sh_omega;
+  if (threadIdx.x == 0)
+    {
+      const double omega = s[1] != 0.0 ? s[0] / s[1] : 0.0; // :488
+      sh_alpha = st->alpha;
+      sh_omega = isfinite (omega) ? omega : NAN;
+      if (blockIdx.x == 0 && !isfinite (omega))
+        {
+          // Leave x untouched so the caller keeps the last finite iterate.
+          st->status = kStateBreakdown;
+          *reinterpret_cast<volatile int *> (&st->done) = 1;
+        }
+    }
+  __syncthreads ();
+  const double omega = sh_omega;
+  if (!isfinite (omega))
+    return;
+  const T ta = (T) sh_alpha, tw = (T) omega;
+  double rhr = 0.0, rr = 0.0;
+  GRID_STRIDE (i, a.n)
+  {
+    const T qi = PRE ? a.q[i] : a.p[i];
+    const T zi = PRE ? a.z[i] : a.s[i];
+    a.x[i] = a.x[i] + ta * qi + tw * zi;     // h = x + alpha q; x = h + omega z
+    const T ri = a.s[i] - tw * a.t[i];       // :340-357
+    a.r[i] = ri;
+    rhr = fma ((double) a.rh[i], (double) ri, rhr);
+    rr = fma ((double) ri, (double) ri, rr);
+  }
+  double vals[2] = { rhr, rr };
+  const int kk[2] = { kRhR, kRR };
+  store_parts<2> (vals, a.part, a.grid, kk);
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    {
+      st->omega = omega;
+      st->rho_prev = st->rho;
+      st->iter = st->iter + 1;
+    }
+}
+
+// Point Jacobi from the diagonal blocks: P = 1/a_rr (1 when |a_rr| < 1e-20
+// or when the row stores no diagonal), gpu/bicgstab.cu:201-225.
+template <typename T>
+__global__ void jacobi_kernel (int nbr, int bs, const int *rp, const int *cols, const T *vals, T *P)
+{
+  GRID_STRIDE (i, (int64_t) nbr * bs)
+  {
+    const int br = (int) (i / bs), r = (int) (i % bs);
+    T d = 1;
+    for (int b = rp[br]; b < rp[br + 1]; b++)
+      if (cols[b] == br)
+        {
+          const T a = vals[(size_t) b * bs * bs + r * bs + r];
+          d = fabs ((double) a) < 1e-20 ? (T) 1 : (T) 1 / a;
+          break;
+        }
+    P[i] = d;
+  }
+}
+
+// ------------------------------------------------------------ dispatch
+
+enum SpmvKind
+{
+  kCsr8,
+  kFlat2,
+  kFlat4,
+  kFlat8,
+  kFlat16,
+  kFlat32,
+  kTpr3,
+  kTprAny
+};
+
+template <typename T, int K> struct OpOf;
+template <typename T> struct OpOf<T, kCsr8> { using type = CsrOp<T, 8>; };
+// Few lanes per block row: every lane then holds whole block lines, so the
+// warp-level FP64 instructions are not spent on predicated-off lanes or on
+// shuffle-reduction adds (each FP64 warp instruction costs the same issue
+// time on GB300's narrow FP64 pipe however many lanes are active).
+template <typename T> struct OpOf<T, kFlat2> { using type = FlatOp<T, 2, 2>; };
+template <typename T> struct OpOf<T, kFlat4> { using type = FlatOp<T, 4, 4>; };
+template <typename T> struct OpOf<T, kFlat8> { using type = FlatOp<T, 8, 4>; };
+template <typename T> struct OpOf<T, kFlat16> { using type = FlatOp<T, 16, 8>; };
+template <typename T> struct OpOf<T, kFlat32> { using type = FlatOp<T, 32, 16>; };
+template <typename T> struct OpOf<T, kTpr3> { using type = TprOp<T, 3>; };
+template <typename T> struct OpOf<T, kTprAny> { using type = TprOp<T, 0>; };
+
+int spmv_kind_for (const bmfp_matrix_s *A)
+{
+  switch (A->bs)
+    {
+    case 0:
+    case 1: return kCsr8;
+    case 2: return kFlat2;
+    case 4: return kFlat4;
+    case 8: return kFlat8;
+    case 16: return kFlat16;
+    case 32: return kFlat32;
+    case 3: return kTpr3;
+    default: return kTprAny;
+    }
+}
+
+template <typename T, int K>
+void launch_spmv_phase (int phase, const Args<T> &a, cudaStream_t s)
+{
+  using Op = typename OpOf<T, K>::type;
+  if (phase == 2)
+    phase_v<T, Op><<<a.grid, kThreads, 0, s>>> (a);
+  else
+    phase_t<T, Op><<<a.grid, kThreads, 0, s>>> (a);
+}
+
+template <typename T>
+void launch_spmv_dispatch (int kind, int phase, const Args<T> &a, cudaStream_t s)
+{
+  switch (kind)
+    {
+    case kCsr8: launch_spmv_phase<T, kCsr8> (phase, a, s); break;
+    case kFlat2: launch_spmv_phase<T, kFlat2> (phase, a, s); break;
+    case kFlat4: launch_spmv_phase<T, kFlat4> (phase, a, s); break;
+    case kFlat8: launch_spmv_phase<T, kFlat8> (phase, a, s); break;
+    case kFlat16: launch_spmv_phase<T, kFlat16> (phase, a, s); break;
+    case kFlat32: launch_spmv_phase<T, kFlat32> (phase, a, s); break;
+    case kTpr3: launch_spmv_phase<T, kTpr3> (phase, a, s); break;
+    default: launch_spmv_phase<T, kTprAny> (phase, a, s); break;
+    }
+}
+
+template <typename T>
+void launch_residual (int kind, const Args<T> &a, const T *x, const T *b, T *r, T *y, cudaStream_t s)
+{
+  switch (kind)
+    {
+#define BMFP_RES(K) case K: residual_kernel<T, typename OpOf<T, K>::type><<<a.grid, kThreads, 0, s>>> (a, x, b, r, y); break;
+      BMFP_RES (kCsr8) BMFP_RES (kFlat2) BMFP_RES (kFlat4) BMFP_RES (kFlat8) BMFP_RES (kFlat16)
+      BMFP_RES (kFlat32) BMFP_RES (kTpr3)
+#undef BMFP_RES
+    default: residual_kernel<T, typename OpOf<T, kTprAny>::type><<<a.grid, kThreads, 0, s>>> (a, x, b, r, y); break;
+    }
+}
+
+template <typename T>
+Args<T> make_args (const bmfp_matrix_s *A, int64_t n, void *x, void *r, void *rh, void *p, void *v,
+                   void *q, void *s, void *z, void *t, void *P, double *part, int grid, DevState *st)
+{
+  Args<T> a;
+  a.nbr = A->n_rows;
+  a.bs = A->bs ? A->bs : 1;
+  a.rp = A->d_row_ptr;
+  a.cols = A->d_cols;
+  a.vals = (const T *) A->d_vals;
+  a.n = n;
+  a.x = (T *) x;
+  a.r = (T *) r;
+  a.rh = (T *) rh;
+  a.p = (T *) p;
+  a.v = (T *) v;
+  a.q = (T *) q;
+  a.s = (T *) s;
+  a.z = (T *) z;
+  a.t = (T *) t;
+  a.P = (const T *) P;
+  a.part = part;
+  a.grid = grid;
+  a.st = st;
+  return a;
+}
+
+template <typename T, bool PRE>
+void launch_vector_phase (int phase, const Args<T> &a, cudaStream_t s)
+{
+  if (phase == 1)
+    phase_p<T, PRE><<<a.grid, kThreads, 0, s>>> (a);
+  else if (phase == 3)
+    phase_s<T, PRE><<<a.grid, kThreads, 0, s>>> (a);
+  else
+    phase_x<T, PRE><<<a.grid, kThreads, 0, s>>> (a);
+}
+} // namespace
+
+// ------------------------------------------------------------ WideEngine
+
+WideEngine::~WideEngine ()
+{
+  if (graph_)
+    cudaGraphExecDestroy (graph_);
+  if (capture_stream_)
+    cudaStreamDestroy (capture_stream_);
+  for (cudaEvent_t e : ev_)
+    if (e)
+      cudaEventDestroy (e);
+  for (void *ptr : { x_, r_, rh_, p_, v_, q_, s_, z_, t_, P_ })
+    cudaFree (ptr);
+  cudaFree (part_);
+  cudaFree (state_);
+  if (h_state_)
+    cudaFreeHost (h_state_);
+}
+
+int WideEngine::init (const bmfp_matrix_s *A, bool jacobi, int chunk, cudaStream_t stream)
+{
+  if (!A)
+    return fail (BMFP_ERROR_INVALID_VALUE, "null matrix");
+  const int bs = A->bs ? A->bs : 1;
+  if (A->bs && A->n_rows != A->n_cols)
+    return fail (BMFP_ERROR_INVALID_VALUE, "BiCGStab needs a square matrix");
+  if (!A->bs && A->n_rows != A->n_cols)
+    return fail (BMFP_ERROR_INVALID_VALUE, "BiCGStab needs a square matrix");
+  A_ = A;
+  dtype_ = A->dtype;
+  jacobi_ = jacobi;
+  chunk_ = std::max (1, std::min (chunk, 256));
+  n_ = (int64_t) A->n_rows * bs;
+  spmv_kind_ = spmv_kind_for (A);
+  // Flat phases need 16-byte aligned values; cudaMalloc'd handles always are.
+  int dev = 0, sms = 0;
+  BMFP_CUDA (cudaGetDevice (&dev));
+  BMFP_CUDA (cudaDeviceGetAttribute (&sms, cudaDevAttrMultiProcessorCount, dev));
+  // Persistent grid: a few CTAs per SM, never more than the rows need.
+  const int64_t want = std::max<int64_t> (1, (n_ + kThreads - 1) / kThreads);
+  grid_ = (int) std::min<int64_t> ((int64_t) sms * 4, want);
+  const size_t S = dtype_size (dtype_);
+  const size_t vb = S * (size_t) std::max<int64_t> (n_, 1);
+  for (void **ptr : { &x_, &r_, &rh_, &p_, &v_, &s_, &t_ })
+    BMFP_CUDA (cudaMalloc (ptr, vb));
+  if (jacobi_)
+    {
+      BMFP_CUDA (cudaMalloc (&q_, vb));
+      BMFP_CUDA (cudaMalloc (&z_, vb));
+      BMFP_CUDA (cudaMalloc (&P_, vb));
+      if (dtype_ == BMFP_R64F)
+        jacobi_kernel<double><<<grid_, kThreads, 0, stream>>> (A->n_rows, bs, A->d_row_ptr, A->d_cols,
+                                                                (const double *) A->d_vals, (double *) P_);
+      else
+        jacobi_kernel<float><<<grid_, kThreads, 0, stream>>> (A->n_rows, bs, A->d_row_ptr, A->d_cols,
+                                                               (const float *) A->d_vals, (float *) P_);
+      BMFP_LAUNCH_CHECK ();
+    }
+  else
+    {
+      q_ = nullptr;
+      z_ = nullptr;
+    }
+  BMFP_CUDA (cudaMalloc (&part_, sizeof (double) * (size_t) kParts * grid_));
+  BMFP_CUDA (cudaMemsetAsync (part_, 0, sizeof (double) * (size_t) kParts * grid_, stream));
+  BMFP_CUDA (cudaMalloc (&state_, sizeof (DevState)));
+  BMFP_CUDA (cudaMemsetAsync (state_, 0, sizeof (DevState), stream));
+  BMFP_CUDA (cudaMallocHost (&h_state_, 2 * sizeof (DevState)));
+  BMFP_CUDA (cudaEventCreateWithFlags (&ev_[0], cudaEventDisableTiming));
+  BMFP_CUDA (cudaEventCreateWithFlags (&ev_[1], cudaEventDisableTiming));
+  BMFP_CUDA (cudaStreamCreateWithFlags (&capture_stream_, cudaStreamNonBlocking));
+  BMFP_CUDA (cudaStreamSynchronize (stream));
+  return capture (capture_stream_);
+}
+
+int WideEngine::launch_phase (int phase, cudaStream_t s)
+{
+  void *q = jacobi_ ? q_ : p_;
+  void *z = jacobi_ ? z_ : s_;
+  if (dtype_ == BMFP_R64F)
+    {
+      Args<double> a = make_args<double> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, part_, grid_, state_);
+      if (phase == 2 || phase == 4)
+        launch_spmv_dispatch<double> (spmv_kind_, phase, a, s);
+      else if (jacobi_)
+        launch_vector_phase<double, true> (phase, a, s);
+      else
+        launch_vector_phase<double, false> (phase, a, s);
+    }
+  else
+    {
+      Args<float> a = make_args<float> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, part_, grid_, state_);
+      if (phase == 2 || phase == 4)
+        launch_spmv_dispatch<float> (spmv_kind_, phase, a, s);
+      else if (jacobi_)
+        launch_vector_phase<float, true> (phase, a, s);
+      else
+        launch_vector_phase<float, false> (phase, a, s);
+    }
+  BMFP_LAUNCH_CHECK ();
+  return BMFP_SUCCESS;
+}
+
+int WideEngine::capture (cudaStream_t s)
+{
+  cudaGraph_t g = nullptr;
+  BMFP_CUDA (cudaStreamBeginCapture (s, cudaStreamCaptureModeThreadLocal));
+  int st = BMFP_SUCCESS;
+  for (int it = 0; it < chunk_ && st == BMFP_SUCCESS; it++)
+    for (int ph = 1; ph <= 5 && st == BMFP_SUCCESS; ph++)
+      st = launch_phase (ph, s);
+  cudaError_t e = cudaStreamEndCapture (s, &g);
+  if (st != BMFP_SUCCESS)
+    {
+      if (g)
+        cudaGraphDestroy (g);
+      return st;
+    }
+  if (e != cudaSuccess)
+    return cuda_fail (e, "cudaStreamEndCapture", __FILE__, __LINE__);
+  e = cudaGraphInstantiate (&graph_, g, 0);
+  cudaGraphDestroy (g);
+  if (e != cudaSuccess)
+    return cuda_fail (e, "cudaGraphInstantiate", __FILE__, __LINE__);
+  return BMFP_SUCCESS;
+}
+
+int WideEngine::start_zero (const void *d_b, double tol, int max_iter, cudaStream_t s)
+{
+  void *q = jacobi_ ? q_ : p_;
+  void *z = jacobi_ ? z_ : s_;
+  if (dtype_ == BMFP_R64F)
+    start_kernel<double, true><<<grid_, kThreads, 0, s>>> (
+      make_args<double> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, part_, grid_, state_),
+      (const double *) d_b, tol, max_iter, -1.0);
+  else
+    start_kernel<float, true><<<grid_, kThreads, 0, s>>> (
+      make_args<float> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, part_, grid_, state_),
+      (const float *) d_b, tol, max_iter, -1.0);
+  BMFP_LAUNCH_CHECK ();
+  return BMFP_SUCCESS;
+}
+
+int WideEngine::start_residual (const void *d_r, double tol, int max_iter_total, double norm_b,
+                                cudaStream_t s)
+{
+  void *q = jacobi_ ? q_ : p_;
+  void *z = jacobi_ ? z_ : s_;
+  if (dtype_ == BMFP_R64F)
+    start_kernel<double, false><<<grid_, kThreads, 0, s>>> (
+      make_args<double> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, part_, grid_, state_),
+      (const double *) d_r, tol, max_iter_total, norm_b);
+  else
+    start_kernel<float, false><<<grid_, kThreads, 0, s>>> (
+      make_args<float> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, part_, grid_, state_),
+      (const float *) d_r, tol, max_iter_total, norm_b);
+  BMFP_LAUNCH_CHECK ();
+  return BMFP_SUCCESS;
+}
+
+int WideEngine::run (cudaStream_t s, DevState *out)
+{
+  // Keep one graph in flight while the host inspects the previous one.
+  long k = 0;
+  const long limit = 1 + (long) 1e9 / chunk_;
+  for (;; k++)
+    {
+      BMFP_CUDA (cudaGraphLaunch (graph_, s));
+      BMFP_CUDA (cudaMemcpyAsync (&h_state_[k & 1], state_, sizeof (DevState), cudaMemcpyDeviceToHost, s));
+      BMFP_CUDA (cudaEventRecord (ev_[k & 1], s));
+      if (k > 0)
+        {
+          BMFP_CUDA (cudaEventSynchronize (ev_[(k - 1) & 1]));
+          if (h_state_[(k - 1) & 1].done)
+            break;
+        }
+      if (k > limit)
+        return fail (BMFP_ERROR_TIMEOUT, "solver did not stop");
+    }
+  BMFP_CUDA (cudaStreamSynchronize (s));
+  *out = h_state_[k & 1];
+  return BMFP_SUCCESS;
+}
+
+int WideEngine::true_residual (const void *d_b, void *d_r, double *rr, double *bb, cudaStream_t s)
+{
+  if (dtype_ == BMFP_R64F)
+    {
+      Args<double> a = make_args<double> (A_, n_, x_, r_, rh_, p_, v_, p_, s_, s_, t_, P_, part_, grid_, state_);
+      launch_residual<double> (spmv_kind_, a, (const double *) x_, (const double *) d_b, (double *) d_r,
+                               (double *) t_, s);
+    }
+  else
+    {
+      Args<float> a = make_args<float> (A_, n_, x_, r_, rh_, p_, v_, p_, s_, s_, t_, P_, part_, grid_, state_);
+      launch_residual<float> (spmv_kind_, a, (const float *) x_, (const float *) d_b, (float *) d_r,
+                              (float *) t_, s);
+    }
+  BMFP_LAUNCH_CHECK ();
+  std::vector<double> h (2 * (size_t) grid_);
+  BMFP_CUDA (cudaMemcpyAsync (h.data (), part_ + (size_t) kResRR * grid_, sizeof (double) * 2 * grid_,
+                              cudaMemcpyDeviceToHost, s));
+  BMFP_CUDA (cudaStreamSynchronize (s));
+  double a = 0.0, b = 0.0;
+  for (int i = 0; i < grid_; i++)
+    {
+      a += h[i];
+      b += h[grid_ + i];
+    }
+  *rr = a;
+  *bb = b;
+  return BMFP_SUCCESS;
+}
+} // namespace bmfp

@@ -8,6 +8,20 @@
 #include <cstddef>
 #include <cstdint>
 
+// A device-resident matrix owned by the library (bmfp_matrix_t).
+struct bmfp_matrix_s
+{
+  int dtype = BMFP_R64F;
+  int n_rows = 0;  // block rows for BCSR, rows for CSR
+  int n_cols = 0;  // block columns for BCSR, columns for CSR
+  int bs = 0;      // 0 = CSR
+  int64_t nnz = 0; // blocks for BCSR, entries for CSR
+  int *d_row_ptr = nullptr;
+  int *d_cols = nullptr;
+  void *d_vals = nullptr;
+  int lanes = 0; // tuned lane count, 0 = heuristic
+};
+
 namespace bmfp
 {
 // Records a printf-style message as the calling thread's last error and
@@ -33,6 +47,8 @@ int spmv_cusparse (int dtype, bool column_major, int n_block_rows, int n_block_c
                    int64_t nnzb, const int *row_ptr, const int *cols, const void *vals,
                    const void *x, void *y, cudaStream_t stream);
 int native_default_lanes (int dtype, int bs, double avg_blocks_per_row);
+int convert_values (int src_dtype, int dst_dtype, int64_t n, const void *src, void *dst,
+                    cudaStream_t stream);
 // Valid lane counts for the native BCSR kernel at this block size, ascending.
 int native_lane_candidates (int dtype, int bs, int *out, int max_out);
 } // namespace bmfp

@@ -1,0 +1,94 @@
+// BiCGStab engines shared by the solver, batch and serving entry points.
+#pragma once
+
+#include "internal.h"
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace bmfp
+{
+// Device-resident scalars of one BiCGStab solve. Every phase kernel reads
+// only fields written by earlier kernels, so no kernel races with itself.
+struct DevState
+{
+  double rho;      // (rh, r) of the current iteration (phase 1)
+  double rho_prev; // previous iteration's rho (phase 5)
+  double alpha;    // phase 3
+  double omega;    // phase 5
+  double norm_b;   // ||r0|| (phase 1, first iteration)
+  double rr;       // last (r, r) seen by phase 1
+  double tol;      // stop when sqrt(rr) / norm_b < tol
+  int iter;        // iterations completed (phase 5)
+  int max_iter;
+  int done;        // set by phase 1; every kernel returns early once set
+  int status;      // 0 running, 1 converged, 2 iteration limit, 3 breakdown
+};
+
+enum
+{
+  kStateRunning = 0,
+  kStateConverged = 1,
+  kStateMaxIter = 2,
+  kStateBreakdown = 3
+};
+
+// Whole-GPU BiCGStab on one matrix: five fused phase kernels per iteration,
+// each over all rows with a fixed persistent grid, captured in a CUDA graph
+// of `chunk` iterations. Dot products are per-CTA partials summed in a fixed
+// order by the next phase, so a solve is deterministic for a given grid.
+class WideEngine
+{
+public:
+  WideEngine () = default;
+  ~WideEngine ();
+  WideEngine (const WideEngine &) = delete;
+  WideEngine &operator= (const WideEngine &) = delete;
+
+  int init (const bmfp_matrix_s *A, bool jacobi, int chunk, cudaStream_t stream);
+  // Start a solve of A x = b from x0 = 0 (b on the device, engine dtype).
+  int start_zero (const void *d_b, double tol, int max_iter, cudaStream_t stream);
+  // Restart from the current x with the residual given in d_r (true residual).
+  // norm_b > 0 sets the reference norm of the convergence test (an engine that
+  // never ran start_zero has none); norm_b <= 0 keeps the previous one.
+  int start_residual (const void *d_r, double tol, int max_iter_total, double norm_b,
+                      cudaStream_t stream);
+  // Run graph chunks until the device sets done; returns the final state.
+  int run (cudaStream_t stream, DevState *out);
+  // r = b - A x, returns ||r||^2 and ||b||^2 (synchronises the stream).
+  int true_residual (const void *d_b, void *d_r, double *rr, double *bb, cudaStream_t stream);
+
+  int dtype () const { return dtype_; }
+  int64_t n () const { return n_; }
+  void *x () const { return x_; }
+  void *scratch () const { return t_; }
+  const bmfp_matrix_s *matrix () const { return A_; }
+
+private:
+  int capture (cudaStream_t stream);
+  int launch_phase (int phase, cudaStream_t stream);
+
+  const bmfp_matrix_s *A_ = nullptr;
+  int dtype_ = BMFP_R64F;
+  bool jacobi_ = false;
+  int64_t n_ = 0;
+  int grid_ = 0;
+  int chunk_ = 16;
+  int spmv_kind_ = 0;
+  void *x_ = nullptr, *r_ = nullptr, *rh_ = nullptr, *p_ = nullptr, *v_ = nullptr;
+  void *q_ = nullptr, *s_ = nullptr, *z_ = nullptr, *t_ = nullptr, *P_ = nullptr;
+  double *part_ = nullptr;
+  DevState *state_ = nullptr;
+  DevState *h_state_ = nullptr; // pinned, two slots
+  cudaGraphExec_t graph_ = nullptr;
+  cudaStream_t capture_stream_ = nullptr;
+  cudaEvent_t ev_[2] = { nullptr, nullptr };
+};
+
+// Elementwise helpers used by the refinement loop (vector_ops.cu).
+int axpy_scaled_convert (int dst_dtype, int src_dtype, int64_t n, double a, const void *src,
+                         void *dst, cudaStream_t stream); // dst += a * src
+int scale_convert (int dst_dtype, int src_dtype, int64_t n, double a, const void *src, void *dst,
+                   cudaStream_t stream);                  // dst = a * src
+} // namespace bmfp

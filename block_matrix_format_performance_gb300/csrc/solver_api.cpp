@@ -1,0 +1,337 @@
+// C ABI of the BiCGStab solver: plain FP64 / FP32 solves and the mixed
+// FP32-inner / FP64-refinement driver, on top of WideEngine (bicgstab.cu).
+#include "solver.h"
+
+#include <chrono>
+#include <cmath>
+#include <memory>
+#include <new>
+
+using namespace bmfp;
+
+struct bmfp_solver_s
+{
+  bmfp_solver_options opts{};
+  const bmfp_matrix_s *A = nullptr;     // the caller's matrix
+  bmfp_matrix_t A_owned = nullptr;      // converted copy (FP32), if any
+  std::unique_ptr<WideEngine> main;     // matrix-precision engine (FP64 for MIXED)
+  std::unique_ptr<WideEngine> inner;    // FP32 engine (MIXED, or FP32 on an FP64 matrix)
+  void *work_a = nullptr;               // residual / converted right-hand side
+  void *work_b = nullptr;
+
+  ~bmfp_solver_s ()
+  {
+    main.reset ();
+    inner.reset ();
+    if (A_owned)
+      bmfp_matrix_destroy (A_owned);
+    cudaFree (work_a);
+    cudaFree (work_b);
+  }
+};
+
+namespace
+{
+int status_of (const DevState &st)
+{
+  if (st.status == kStateConverged)
+    return BMFP_SUCCESS;
+  if (st.status == kStateBreakdown)
+    return BMFP_ERROR_BREAKDOWN;
+  return BMFP_ERROR_NOT_CONVERGED;
+}
+
+// Solve with one engine from x0 = 0, then (optionally) verify the true
+// residual and restart from it while the recursive residual stopped early.
+int solve_plain (WideEngine &e, const void *d_b, void *d_r, const bmfp_solver_options &o,
+                 bmfp_solve_info *info, cudaStream_t s)
+{
+  DevState st{};
+  int rc = e.start_zero (d_b, o.tolerance, o.max_iterations, s);
+  if (rc == BMFP_SUCCESS)
+    rc = e.run (s, &st);
+  if (rc != BMFP_SUCCESS)
+    return rc;
+  int status = status_of (st);
+  double rel_true = NAN, prev_rel = INFINITY;
+  int restarts = 0;
+  if (o.check_true_residual)
+    for (;;)
+      {
+        double rr = 0, bb = 0;
+        rc = e.true_residual (d_b, d_r, &rr, &bb, s);
+        if (rc != BMFP_SUCCESS)
+          return rc;
+        rel_true = bb > 0 ? std::sqrt (rr / bb) : 0.0;
+        if (rel_true < o.tolerance)
+          {
+            status = BMFP_SUCCESS;
+            break;
+          }
+        status = st.status == kStateBreakdown ? BMFP_ERROR_BREAKDOWN : BMFP_ERROR_NOT_CONVERGED;
+        // Restart from the true residual while that still gains accuracy; a
+        // restart that does not halve it means the attainable accuracy of the
+        // working precision has been reached.
+        if (st.status != kStateConverged || st.iter >= o.max_iterations || restarts >= 8
+            || !(rel_true < 0.5 * prev_rel))
+          break;
+        prev_rel = rel_true;
+        restarts++;
+        rc = e.start_residual (d_r, o.tolerance, o.max_iterations, -1.0, s);
+        if (rc == BMFP_SUCCESS)
+          rc = e.run (s, &st);
+        if (rc != BMFP_SUCCESS)
+          return rc;
+      }
+  info->status = status;
+  info->iterations += st.iter;
+  info->restarts += restarts;
+  info->true_rel_residual = rel_true;
+  info->recursive_rel_residual = st.norm_b > 0 ? std::sqrt (st.rr) / st.norm_b : 0.0;
+  return BMFP_SUCCESS;
+}
+
+int solve_mixed (bmfp_solver_s *sv, const void *d_b, bmfp_solve_info *info, cudaStream_t s)
+{
+  const bmfp_solver_options &o = sv->opts;
+  WideEngine &e64 = *sv->main;
+  WideEngine &e32 = *sv->inner;
+  const int64_t n = e64.n ();
+  void *r64 = sv->work_a; // FP64 residual
+  void *r32 = sv->work_b; // scaled FP32 right-hand side of the inner solve
+  BMFP_CUDA (cudaMemsetAsync (e64.x (), 0, sizeof (double) * (size_t) n, s));
+  double prev_rel = INFINITY;
+  int iters64 = 0, iters32 = 0;
+  for (int k = 0;; k++)
+    {
+      double rr = 0, bb = 0;
+      int rc = e64.true_residual (d_b, r64, &rr, &bb, s);
+      if (rc != BMFP_SUCCESS)
+        return rc;
+      const double rel = bb > 0 ? std::sqrt (rr / bb) : 0.0;
+      info->true_rel_residual = rel;
+      info->recursive_rel_residual = rel;
+      if (rel < o.tolerance)
+        {
+          info->status = BMFP_SUCCESS;
+          break;
+        }
+      const bool budget_left = iters64 + iters32 < o.max_iterations && k < o.max_refinements;
+      const bool stalled = k > 0 && rel > prev_rel / 4;
+      if (!budget_left || (stalled && o.fallback_fp64))
+        {
+          if (!o.fallback_fp64 || iters64 + iters32 >= o.max_iterations)
+            {
+              info->status = BMFP_ERROR_NOT_CONVERGED;
+              break;
+            }
+          // Finish in FP64 from the current x (restart from its true residual).
+          info->used_fp64_fallback = 1;
+          DevState st{};
+          rc = e64.start_residual (r64, o.tolerance, o.max_iterations - iters32, std::sqrt (bb), s);
+          if (rc == BMFP_SUCCESS)
+            rc = e64.run (s, &st);
+          if (rc != BMFP_SUCCESS)
+            return rc;
+          iters64 = st.iter;
+          int restarts = 0;
+          double last = INFINITY;
+          for (;;)
+            {
+              rc = e64.true_residual (d_b, r64, &rr, &bb, s);
+              if (rc != BMFP_SUCCESS)
+                return rc;
+              info->true_rel_residual = bb > 0 ? std::sqrt (rr / bb) : 0.0;
+              info->recursive_rel_residual = st.norm_b > 0 ? std::sqrt (st.rr) / st.norm_b : 0.0;
+              if (info->true_rel_residual < o.tolerance)
+                {
+                  info->status = BMFP_SUCCESS;
+                  break;
+                }
+              info->status = st.status == kStateBreakdown ? BMFP_ERROR_BREAKDOWN : BMFP_ERROR_NOT_CONVERGED;
+              if (st.status != kStateConverged || restarts >= 8 || iters64 + iters32 >= o.max_iterations
+                  || !(info->true_rel_residual < 0.5 * last))
+                break;
+              last = info->true_rel_residual;
+              restarts++;
+              rc = e64.start_residual (r64, o.tolerance, o.max_iterations - iters32, -1.0, s);
+              if (rc == BMFP_SUCCESS)
+                rc = e64.run (s, &st);
+              if (rc != BMFP_SUCCESS)
+                return rc;
+              iters64 = st.iter;
+            }
+          info->restarts += restarts;
+          break;
+        }
+      prev_rel = rel;
+      // Inner FP32 solve of A d = r / ||r||, then x += ||r|| d in FP64.
+      const double scale = std::sqrt (rr);
+      rc = scale_convert (BMFP_R32F, BMFP_R64F, n, 1.0 / scale, r64, r32, s);
+      if (rc != BMFP_SUCCESS)
+        return rc;
+      DevState st{};
+      const int cap = std::min (o.inner_max_iterations, o.max_iterations - iters64 - iters32);
+      rc = e32.start_zero (r32, o.inner_tolerance, cap, s);
+      if (rc == BMFP_SUCCESS)
+        rc = e32.run (s, &st);
+      if (rc != BMFP_SUCCESS)
+        return rc;
+      iters32 += st.iter;
+      info->refinements = k + 1;
+      if (st.status == kStateBreakdown && !(st.norm_b > 0 && std::sqrt (st.rr) < 0.5 * st.norm_b))
+        {
+          // The FP32 inner solve broke down without halving its residual: do
+          // not apply it; the next pass falls back to FP64.
+          prev_rel = 0.0;
+          continue;
+        }
+      rc = axpy_scaled_convert (BMFP_R64F, BMFP_R32F, n, scale, e32.x (), e64.x (), s);
+      if (rc != BMFP_SUCCESS)
+        return rc;
+    }
+  info->iterations = iters64 + iters32;
+  info->iterations_fp32 = iters32;
+  return BMFP_SUCCESS;
+}
+} // namespace
+
+extern "C" {
+
+void bmfp_solver_options_init (bmfp_solver_options *o)
+{
+  if (!o)
+    return;
+  o->precision = BMFP_SOLVE_FP64;
+  o->preconditioner = BMFP_PRECOND_NONE;
+  o->tolerance = 1e-10;
+  o->max_iterations = 100000;
+  o->check_true_residual = 1;
+  o->inner_tolerance = 1e-4;
+  o->inner_max_iterations = 1000;
+  o->max_refinements = 30;
+  o->fallback_fp64 = 1;
+  o->iterations_per_graph = 16;
+}
+
+int bmfp_solver_create (bmfp_solver_t *out, bmfp_matrix_t A, const bmfp_solver_options *opts,
+                        void *stream)
+{
+  if (!out || !A)
+    return fail (BMFP_ERROR_INVALID_VALUE, "null argument");
+  *out = nullptr;
+  bmfp_solver_options o;
+  bmfp_solver_options_init (&o);
+  if (opts)
+    o = *opts;
+  if (o.precision < BMFP_SOLVE_FP64 || o.precision > BMFP_SOLVE_MIXED)
+    return fail (BMFP_ERROR_INVALID_VALUE, "invalid precision %d", o.precision);
+  if (o.preconditioner != BMFP_PRECOND_NONE && o.preconditioner != BMFP_PRECOND_JACOBI)
+    return fail (BMFP_ERROR_INVALID_VALUE, "invalid preconditioner %d", o.preconditioner);
+  if (!(o.tolerance > 0) || o.max_iterations < 0 || o.iterations_per_graph < 1)
+    return fail (BMFP_ERROR_INVALID_VALUE, "invalid tolerance or iteration limits");
+  if (o.precision == BMFP_SOLVE_MIXED && A->dtype != BMFP_R64F)
+    return fail (BMFP_ERROR_INVALID_VALUE, "mixed precision needs an FP64 matrix");
+  if (o.precision == BMFP_SOLVE_FP64 && A->dtype != BMFP_R64F)
+    return fail (BMFP_ERROR_INVALID_VALUE, "FP64 solves need an FP64 matrix");
+  const int n_rows = A->n_rows * (A->bs ? A->bs : 1);
+  const int n_cols = A->n_cols * (A->bs ? A->bs : 1);
+  if (n_rows != n_cols)
+    return fail (BMFP_ERROR_INVALID_VALUE, "BiCGStab needs a square matrix (%d x %d)", n_rows, n_cols);
+  cudaStream_t s = as_stream (stream);
+  std::unique_ptr<bmfp_solver_s> sv (new (std::nothrow) bmfp_solver_s);
+  if (!sv)
+    return fail (BMFP_ERROR_OUT_OF_MEMORY, "host allocation failed");
+  sv->opts = o;
+  sv->A = A;
+  const bool jac = o.preconditioner == BMFP_PRECOND_JACOBI;
+  int rc = BMFP_SUCCESS;
+  const bmfp_matrix_s *A32 = A;
+  if (o.precision != BMFP_SOLVE_FP64 && A->dtype == BMFP_R64F)
+    {
+      rc = bmfp_matrix_convert (&sv->A_owned, A, BMFP_R32F, stream);
+      if (rc != BMFP_SUCCESS)
+        return rc;
+      A32 = sv->A_owned;
+    }
+  if (o.precision == BMFP_SOLVE_FP32)
+    {
+      sv->main.reset (new (std::nothrow) WideEngine);
+      rc = sv->main->init (A32, jac, o.iterations_per_graph, s);
+    }
+  else
+    {
+      sv->main.reset (new (std::nothrow) WideEngine);
+      rc = sv->main->init (A, jac, o.iterations_per_graph, s);
+      if (rc == BMFP_SUCCESS && o.precision == BMFP_SOLVE_MIXED)
+        {
+          sv->inner.reset (new (std::nothrow) WideEngine);
+          rc = sv->inner->init (A32, jac, o.iterations_per_graph, s);
+        }
+    }
+  if (rc != BMFP_SUCCESS)
+    return rc;
+  const size_t nb = (size_t) std::max (n_rows, 1);
+  BMFP_CUDA (cudaMalloc (&sv->work_a, nb * 8));
+  BMFP_CUDA (cudaMalloc (&sv->work_b, nb * 8));
+  *out = sv.release ();
+  return BMFP_SUCCESS;
+}
+
+int bmfp_solver_solve (bmfp_solver_t sv, const void *d_b, void *d_x, bmfp_solve_info *info_out,
+                       void *stream)
+{
+  if (!sv || !d_b || !d_x)
+    return fail (BMFP_ERROR_INVALID_VALUE, "null argument");
+  cudaStream_t s = as_stream (stream);
+  bmfp_solve_info info{};
+  const auto t0 = std::chrono::steady_clock::now ();
+  int rc = BMFP_SUCCESS;
+  const int64_t n = sv->main->n ();
+  const int user_dtype = sv->A->dtype;
+  if (sv->opts.precision == BMFP_SOLVE_MIXED)
+    {
+      rc = solve_mixed (sv, d_b, &info, s);
+      if (rc == BMFP_SUCCESS)
+        rc = convert_values (BMFP_R64F, user_dtype, n, sv->main->x (), d_x, s);
+    }
+  else
+    {
+      WideEngine &e = *sv->main;
+      const void *b = d_b;
+      if (e.dtype () != user_dtype)
+        {
+          rc = convert_values (user_dtype, e.dtype (), n, d_b, sv->work_b, s);
+          b = sv->work_b;
+        }
+      if (rc == BMFP_SUCCESS)
+        rc = solve_plain (e, b, sv->work_a, sv->opts, &info, s);
+      if (e.dtype () == BMFP_R32F)
+        info.iterations_fp32 = info.iterations;
+      if (rc == BMFP_SUCCESS)
+        rc = convert_values (e.dtype (), user_dtype, n, e.x (), d_x, s);
+    }
+  if (rc == BMFP_SUCCESS)
+    {
+      cudaError_t e = cudaStreamSynchronize (s);
+      if (e != cudaSuccess)
+        rc = cuda_fail (e, "solve", __FILE__, __LINE__);
+    }
+  info.seconds = std::chrono::duration<double> (std::chrono::steady_clock::now () - t0).count ();
+  if (info_out)
+    *info_out = info;
+  if (rc != BMFP_SUCCESS)
+    return rc;
+  if (info.status != BMFP_SUCCESS)
+    fail (info.status, "BiCGStab stopped with status %d after %d iterations (true residual %.3e)",
+          info.status, info.iterations, info.true_rel_residual);
+  return info.status;
+}
+
+int bmfp_solver_destroy (bmfp_solver_t sv)
+{
+  delete sv;
+  return BMFP_SUCCESS;
+}
+
+} // extern "C"

@@ -26,8 +26,8 @@
 // Values are loaded with the streaming (evict-first) hint, x through the
 // read-only path. No tensor cores: a single-vector product has no reuse of A
 // to feed them.
-#include "device_common.cuh"
 #include "internal.h"
+#include "spmv_core.cuh"
 
 #include <algorithm>
 
@@ -37,195 +37,31 @@ namespace
 {
 constexpr int kThreads = 256;
 
+// Grid-stride over block rows: group g takes rows g, g + n_groups, ...
 template <typename T, int BS, int G, int U>
 __global__ void __launch_bounds__ (kThreads)
   bcsr_flat_kernel (int n_block_rows, const int *__restrict__ row_ptr,
                     const int *__restrict__ cols, const T *__restrict__ vals,
                     const T *__restrict__ x, T *__restrict__ y)
 {
-  using V16 = dev::Vec16<T>;
-  constexpr int V = V16::N;
-  constexpr int E = BS * BS;
-  constexpr int CH = G * V; // elements one group iteration covers
-  static_assert (E % V == 0, "a block must be a whole number of 16-byte vectors");
-  static_assert (CH >= BS, "a group chunk must cover at least one block line");
-
-  const int64_t tid = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
-  const int group = (int) (tid / G);
-  const int gl = threadIdx.x & (G - 1);
-  if (group >= n_block_rows)
-    return; // groups are lane-aligned, so a whole group leaves together
-  const unsigned mask = dev::group_mask<G> ();
-
-  const int beg = __ldg (row_ptr + group);
-  const int nblk = __ldg (row_ptr + group + 1) - beg;
-  const T *vb = vals + (size_t) beg * E;
-  const int *cb = cols + beg;
-
-  if constexpr (CH >= E)
-    {
-      constexpr int BPI = CH / E; // whole blocks per group iteration
-      const int bl = (gl * V) / E;
-      const int o = (gl * V) % E;
-      if constexpr (V <= BS)
-        {
-          // V consecutive values of one block line: row o/BS, columns c0..c0+V-1.
-          const int c0 = o % BS;
-          T acc = 0;
-          for (int b0 = 0; b0 < nblk; b0 += BPI * U)
-            {
-              V16 a[U];
-              int c[U];
-#pragma unroll
-              for (int u = 0; u < U; u++)
-                {
-                  const int b = b0 + u * BPI + bl;
-                  c[u] = -1;
-                  if (b < nblk)
-                    {
-                      a[u] = dev::ld_stream16 (vb + b * E + o);
-                      c[u] = __ldg (cb + b);
-                    }
-                }
-#pragma unroll
-              for (int u = 0; u < U; u++)
-                if (c[u] >= 0)
-                  {
-                    const V16 xv = dev::ld_cached16 (x + (size_t) c[u] * BS + c0);
-#pragma unroll
-                    for (int v = 0; v < V; v++)
-                      acc = fma (a[u].v[v], xv.v[v], acc);
-                  }
-            }
-          // Sum over the column-group bits (below BS/V) and the block bits
-          // (E/V and above); the row bits in between stay distinct.
-#pragma unroll
-          for (int off = 1; off < BS / V; off <<= 1)
-            acc += __shfl_xor_sync (mask, acc, off);
-#pragma unroll
-          for (int off = E / V; off < G; off <<= 1)
-            acc += __shfl_xor_sync (mask, acc, off);
-          if (gl < E / V && (gl % (BS / V)) == 0)
-            y[(size_t) group * BS + gl / (BS / V)] = acc;
-        }
-      else
-        {
-          // V > BS only for bs = 2 in float: one vector is a whole block
-          // (a00 a01 a10 a11).
-          static_assert (V == E, "unexpected vector/block shape");
-          T acc0 = 0, acc1 = 0;
-          for (int b0 = 0; b0 < nblk; b0 += BPI * U)
-            {
-              V16 a[U];
-              int c[U];
-#pragma unroll
-              for (int u = 0; u < U; u++)
-                {
-                  const int b = b0 + u * BPI + bl;
-                  c[u] = -1;
-                  if (b < nblk)
-                    {
-                      a[u] = dev::ld_stream16 (vb + b * E);
-                      c[u] = __ldg (cb + b);
-                    }
-                }
-#pragma unroll
-              for (int u = 0; u < U; u++)
-                if (c[u] >= 0)
-                  {
-                    T x0, x1;
-                    dev::ld_cached2 (x + (size_t) c[u] * 2, x0, x1);
-                    acc0 = fma (a[u].v[0], x0, acc0);
-                    acc0 = fma (a[u].v[1], x1, acc0);
-                    acc1 = fma (a[u].v[2], x0, acc1);
-                    acc1 = fma (a[u].v[3], x1, acc1);
-                  }
-            }
-          acc0 = dev::group_sum<G> (acc0);
-          acc1 = dev::group_sum<G> (acc1);
-          if (gl == 0)
-            {
-              y[(size_t) group * 2] = acc0;
-              y[(size_t) group * 2 + 1] = acc1;
-            }
-        }
-    }
-  else
-    {
-      // Large blocks: NP phases per block; in phase p lane l holds row
-      // p*RPP + (l*V)/BS, columns c0..c0+V-1 with c0 = (l*V) % BS.
-      constexpr int NP = E / CH;
-      constexpr int RPP = CH / BS;
-      const int c0 = (gl * V) % BS;
-      const int rl = (gl * V) / BS;
-      T acc[NP];
-#pragma unroll
-      for (int p = 0; p < NP; p++)
-        acc[p] = 0;
-#pragma unroll 2
-      for (int b = 0; b < nblk; b++)
-        {
-          const T *blk = vb + b * E + gl * V;
-          V16 a[NP];
-#pragma unroll
-          for (int p = 0; p < NP; p++)
-            a[p] = dev::ld_stream16 (blk + p * CH);
-          const int c = __ldg (cb + b);
-          const V16 xv = dev::ld_cached16 (x + (size_t) c * BS + c0);
-#pragma unroll
-          for (int p = 0; p < NP; p++)
-#pragma unroll
-            for (int v = 0; v < V; v++)
-              acc[p] = fma (a[p].v[v], xv.v[v], acc[p]);
-        }
-#pragma unroll
-      for (int p = 0; p < NP; p++)
-#pragma unroll
-        for (int off = 1; off < BS / V; off <<= 1)
-          acc[p] += __shfl_xor_sync (mask, acc[p], off);
-      if ((gl % (BS / V)) == 0)
-#pragma unroll
-        for (int p = 0; p < NP; p++)
-          y[(size_t) group * BS + p * RPP + rl] = acc[p];
-    }
+  const int64_t group = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int64_t n_groups = (int64_t) gridDim.x * blockDim.x / G;
+  core::NoEpilogue epi;
+  for (int64_t row = group; row < n_block_rows; row += n_groups)
+    core::flat_row<T, BS, G, U> ((int) row, row_ptr, cols, vals, x, y, epi);
 }
 
-// Warp per block row, lane (q, r) = (lane / bs, lane % bs) for q < 32/bs.
 template <typename T, int BSC>
 __global__ void __launch_bounds__ (kThreads)
   bcsr_tpr_kernel (int n_block_rows, int bs_rt, const int *__restrict__ row_ptr,
                    const int *__restrict__ cols, const T *__restrict__ vals,
                    const T *__restrict__ x, T *__restrict__ y)
 {
-  const int bs = BSC ? BSC : bs_rt;
-  const int Q = 32 / bs;
-  const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (warp >= n_block_rows)
-    return; // whole warp
-  const int q = lane / bs, r = lane % bs;
-  const bool live = q < Q;
-  const int beg = __ldg (row_ptr + warp), end = __ldg (row_ptr + warp + 1);
-  T acc = 0;
-  if (live)
-    for (int b = beg + q; b < end; b += Q)
-      {
-        const T *a = vals + (size_t) b * bs * bs + r * bs;
-        const T *xb = x + (size_t) __ldg (cols + b) * bs;
-        for (int c = 0; c < bs; c++)
-          acc = fma (dev::ld_stream (a + c), dev::ld_cached (xb + c), acc);
-      }
-  int top = 1;
-  while (top < Q)
-    top <<= 1;
-  for (int s = top >> 1; s > 0; s >>= 1)
-    {
-      const T other = __shfl_down_sync (0xffffffffu, acc, s * bs);
-      if (live && q + s < Q)
-        acc += other;
-    }
-  if (q == 0)
-    y[(size_t) warp * bs + r] = acc;
+  const int64_t n_warps = (int64_t) gridDim.x * blockDim.x >> 5;
+  core::NoEpilogue epi;
+  for (int64_t row = warp; row < n_block_rows; row += n_warps)
+    core::tpr_row<T, BSC> ((int) row, bs_rt, row_ptr, cols, vals, x, y, epi);
 }
 
 // Thread per scalar row (bs > 32).
@@ -256,26 +92,11 @@ __global__ void __launch_bounds__ (kThreads)
   csr_subwarp_kernel (int n_rows, const int *__restrict__ row_ptr, const int *__restrict__ cols,
                       const T *__restrict__ vals, const T *__restrict__ x, T *__restrict__ y)
 {
-  const int64_t tid = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t row = tid / G;
-  const int gl = threadIdx.x & (G - 1);
-  if (row >= n_rows)
-    return;
-  const int beg = __ldg (row_ptr + row), end = __ldg (row_ptr + row + 1);
-  T acc0 = 0, acc1 = 0;
-  int e = beg + gl;
-  for (; e + G < end; e += 2 * G)
-    {
-      const T a0 = dev::ld_stream (vals + e), a1 = dev::ld_stream (vals + e + G);
-      const int c0 = __ldg (cols + e), c1 = __ldg (cols + e + G);
-      acc0 = fma (a0, dev::ld_cached (x + c0), acc0);
-      acc1 = fma (a1, dev::ld_cached (x + c1), acc1);
-    }
-  if (e < end)
-    acc0 = fma (dev::ld_stream (vals + e), dev::ld_cached (x + __ldg (cols + e)), acc0);
-  T acc = dev::group_sum<G> (acc0 + acc1);
-  if (gl == 0)
-    y[row] = acc;
+  const int64_t group = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int64_t n_groups = (int64_t) gridDim.x * blockDim.x / G;
+  core::NoEpilogue epi;
+  for (int64_t row = group; row < n_rows; row += n_groups)
+    core::csr_row<T, G> ((int) row, row_ptr, cols, vals, x, y, epi);
 }
 
 // ---------------------------------------------------------------- dispatch
@@ -405,6 +226,21 @@ int native_default_lanes (int dtype, int bs, double avg_blocks_per_row)
     return csr_default_lanes (avg_blocks_per_row);
   if (!flat_bs (bs))
     return 32;
+  if (dtype == BMFP_R64F)
+    {
+      // FP64 products are bound by GB300's narrow FP64 pipe, where a warp
+      // instruction costs the same whether 2 or 32 lanes are active: give
+      // each lane whole block lines (no predicated-off lanes, few shuffle
+      // adds): bs 2 -> 2 lanes, 4 -> 4, 8 -> 4, 16 -> 8, 32 -> 16.
+      switch (bs)
+        {
+        case 2: return 2;
+        case 4: return 4;
+        case 8: return 4;
+        case 16: return 8;
+        default: return 16;
+        }
+    }
   // Aim for about two 16-byte vectors per lane per block row, within the
   // lane counts this block size allows.
   const double vectors = avg_blocks_per_row * bs * bs / vec_elems (dtype);

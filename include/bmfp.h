@@ -197,6 +197,78 @@ BMFP_API int bmfp_matrix_spmv (bmfp_matrix_t m, const void *d_x, void *d_y, void
 BMFP_API int bmfp_matrix_autotune (bmfp_matrix_t m, const void *d_x, void *d_y, void *stream,
                                    int *chosen_lanes);
 
+/* ------------------------------------------------------------- BiCGStab ---
+ * Replaces gpu_bicgstab<T,C> (gpu/bicgstab.h:10-16, gpu/bicgstab.cu:23-526):
+ * the same recurrences and optional point-Jacobi right preconditioning, with
+ * the scalars kept on the device, the vector updates and dot products fused
+ * into five phase kernels per iteration and the iterations launched as CUDA
+ * graphs. A solver is bound to one matrix handle; solves may be repeated with
+ * different right-hand sides. */
+enum bmfp_solve_precision
+{
+  BMFP_SOLVE_FP64 = 0,  /* FP64 matrix, vectors and recurrences */
+  BMFP_SOLVE_FP32 = 1,  /* FP32 matrix (converted if needed), vectors and recurrences */
+  BMFP_SOLVE_MIXED = 2  /* FP32 inner BiCGStab on an FP32 copy of the matrix; true
+                           residual b - A x, solution update and the outer
+                           convergence norm in FP64 (iterative refinement) */
+};
+
+enum bmfp_preconditioner
+{
+  BMFP_PRECOND_NONE = 0,
+  BMFP_PRECOND_JACOBI = 1 /* P = 1/a_ii from the diagonal blocks, bicgstab.cu:201-238 */
+};
+
+typedef struct bmfp_solver_options
+{
+  int precision;            /* enum bmfp_solve_precision */
+  int preconditioner;       /* enum bmfp_preconditioner */
+  double tolerance;         /* target ||b - A x|| / ||b|| */
+  int max_iterations;       /* BiCGStab iterations in total (FP64 and FP32) */
+  int check_true_residual;  /* 1 (default): at the end verify b - A x in the matrix
+                               precision and restart from it while it is above
+                               tolerance; 0: stop on the recursive residual only,
+                               as gpu/bicgstab.cu:512 does */
+  double inner_tolerance;   /* MIXED: residual reduction asked of each FP32 inner solve */
+  int inner_max_iterations; /* MIXED: iteration cap of one inner solve */
+  int max_refinements;      /* MIXED: outer refinement steps */
+  int fallback_fp64;        /* MIXED: when an outer step cuts the FP64 residual by less
+                               than 4x, finish with FP64 BiCGStab from the current x */
+  int iterations_per_graph; /* BiCGStab iterations per CUDA graph launch */
+} bmfp_solver_options;
+
+typedef struct bmfp_solve_info
+{
+  int status;                    /* BMFP_SUCCESS, BMFP_ERROR_NOT_CONVERGED or BMFP_ERROR_BREAKDOWN */
+  int iterations;                /* all BiCGStab iterations */
+  int iterations_fp32;           /* of which FP32 (inner) iterations */
+  int refinements;               /* MIXED outer steps */
+  int restarts;                  /* restarts from the true residual */
+  int used_fp64_fallback;        /* MIXED finished in FP64 */
+  double true_rel_residual;      /* ||b - A x|| / ||b||, computed in the matrix precision */
+  double recursive_rel_residual; /* BiCGStab's own residual at exit */
+  double seconds;                /* host wall time of the solve */
+} bmfp_solve_info;
+
+typedef struct bmfp_solver_s *bmfp_solver_t;
+
+/* Defaults: FP64, no preconditioner, tolerance 1e-10, 100000 iterations,
+ * true-residual check on, inner tolerance 1e-4, 1000 inner iterations,
+ * 30 refinements, FP64 fallback on, 16 iterations per graph. */
+BMFP_API void bmfp_solver_options_init (bmfp_solver_options *opts);
+/* Allocate the Krylov vectors and capture the iteration graph. The matrix must
+ * be square and must outlive the solver (for MIXED it must be FP64). This call
+ * synchronises the stream; the reference constructor's 80 %-of-memory guard
+ * (bicgstab.cu:41-42) becomes BMFP_ERROR_OUT_OF_MEMORY from the allocations. */
+BMFP_API int bmfp_solver_create (bmfp_solver_t *out, bmfp_matrix_t A, const bmfp_solver_options *opts,
+                                 void *stream);
+/* Solve A x = b from x0 = 0. b and x are device vectors of the matrix dtype
+ * (FP64 for MIXED). Blocks until the solve ends; x holds the last iterate
+ * whatever the status. Returns info->status. */
+BMFP_API int bmfp_solver_solve (bmfp_solver_t s, const void *d_b, void *d_x, bmfp_solve_info *info,
+                                void *stream);
+BMFP_API int bmfp_solver_destroy (bmfp_solver_t s);
+
 /* --------------------------------------------------- host-side utilities ---
  * Pure host functions (no GPU needed). */
 

@@ -1,0 +1,173 @@
+"""BiCGStab on the GPU against the oracle's restatement of the reference loop
+(gpu/bicgstab.cu:387-513) and an independent FP64 direct solve.
+
+Bars: true relative residual ||b - A x|| / ||b|| below the tolerance, error
+against the direct solve reported and bounded, iteration counts within 25 %
+(+10) of the oracle's (the dot products sum in a different order; BiCGStab's
+erratic residual history on these operators turns that into a different
+iteration count, most visibly with Jacobi), and bitwise repeatability.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as sla
+
+import block_matrix_format_performance_gb300 as bm
+
+pytestmark = pytest.mark.gpu
+
+
+def dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def bcsr_dense_csr(rp, c, v, bs):
+    crp, cc, cv = bm.bcsr_to_csr(rp, c, v, bs)
+    n = (len(rp) - 1) * bs
+    return sp.csr_matrix((cv, cc, crp), shape=(n, n))
+
+
+def diag_dominant_bcsr(nbr, bs, seed, extra=8):
+    """Random BCSR with a dominant diagonal block in every block row."""
+    rng = np.random.default_rng(seed)
+    rows = []
+    for i in range(nbr):
+        cand = np.unique(np.concatenate([[i], rng.integers(max(0, i - 20), min(nbr, i + 21), extra)]))
+        rows.append(cand)
+    rp = np.concatenate([[0], np.cumsum([len(r) for r in rows])]).astype(np.int32)
+    c = np.concatenate(rows).astype(np.int32)
+    v = rng.uniform(-1, 1, c.size * bs * bs)
+    for i in range(nbr):
+        k = rp[i] + int(np.where(rows[i] == i)[0][0])
+        blk = v[k * bs * bs:(k + 1) * bs * bs].reshape(bs, bs)
+        blk += np.eye(bs) * (len(rows[i]) * bs * 1.5)
+    return rp, c, v
+
+
+@pytest.mark.parametrize("precond", ["none", "jacobi"])
+@pytest.mark.parametrize("grid", [(24, 6), (50, 13), (100, 25)])
+def test_fp64_q4_elasticity_matches_oracle(lib, orc, cuda, grid, precond):
+    nx, ny = grid
+    rp, c, v, rhs = bm.gen_q4_elasticity(nx, ny)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    s = bm.Solver(A, "fp64", tol=1e-10, max_iters=50000, preconditioner=precond)
+    x, info = s.solve_host(rhs)
+    K = bcsr_dense_csr(rp, c, v, 2)
+    rel = np.linalg.norm(rhs - K @ x) / np.linalg.norm(rhs)
+    assert info["status"] == bm.SUCCESS, info
+    assert rel < 1e-10 and abs(rel - info["true_rel_residual"]) <= 1e-12 + 1e-3 * rel
+    xd = sla.spsolve(K.tocsc(), rhs)
+    err = np.linalg.norm(x - xd) / np.linalg.norm(xd)
+    assert err < 1e-5, err  # reported: forward error bounded by cond(A) * residual
+    crp, cc, cv = orc.bcsr_to_csr(rp, c, v, 2)
+    xo, st, it_o, _ = orc.bicgstab(crp, cc, cv, rhs, 1e-10, 50000, precond == "jacobi")
+    it_first = info["iterations"]
+    assert abs(it_first - it_o) <= 0.25 * it_o + 10 + 50 * info["restarts"], (it_first, it_o, info)
+    s.close(), A.close()
+
+
+def test_recursive_only_mode_follows_reference_stop_rule(lib, orc, cuda):
+    # check_true_residual = 0: stop when ||r_i|| / ||b|| < eps (gpu/bicgstab.cu:512)
+    rp, c, v, rhs = bm.gen_q4_elasticity(40, 10)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    s = bm.Solver(A, "fp64", tol=1e-8, max_iters=10000, check_true_residual=False)
+    x, info = s.solve_host(rhs)
+    crp, cc, cv = orc.bcsr_to_csr(rp, c, v, 2)
+    _, st, it_o, rr_o = orc.bicgstab(crp, cc, cv, rhs, 1e-8, 10000, False)
+    assert info["status"] == bm.SUCCESS and info["recursive_rel_residual"] < 1e-8
+    assert abs(info["iterations"] - it_o) <= 0.25 * it_o + 10
+    assert info["restarts"] == 0
+
+
+def test_solve_is_bitwise_repeatable(lib, cuda):
+    rp, c, v, rhs = bm.gen_q4_elasticity(60, 15)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    s = bm.Solver(A, "fp64")
+    x1, i1 = s.solve_host(rhs)
+    x2, i2 = s.solve_host(rhs)
+    assert i1["iterations"] == i2["iterations"]
+    assert np.array_equal(x1.view(np.uint64), x2.view(np.uint64))
+
+
+@pytest.mark.parametrize("bs", [1, 2, 3, 4, 8])
+def test_fp64_diag_dominant_any_block_size(lib, cuda, bs):
+    rp, c, v = diag_dominant_bcsr(300, bs, seed=bs)
+    K = bcsr_dense_csr(rp, c, v, bs)
+    b = np.random.default_rng(1).uniform(-1, 1, 300 * bs)
+    A = bm.Matrix.from_bcsr(rp, c, v, bs)
+    x, info = bm.Solver(A, "fp64").solve_host(b)
+    assert info["status"] == bm.SUCCESS
+    assert np.linalg.norm(b - K @ x) / np.linalg.norm(b) < 1e-10
+    xd = sla.spsolve(K.tocsc(), b)
+    assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 1e-9
+
+
+def test_csr_matrix_solve_like_the_reference(lib, orc, cuda):
+    """The reference solves CSR (csr_matrix_class); bs = 0 handles go through
+    the CSR phase kernels."""
+    rp, c, v, rhs = bm.gen_q4_elasticity(30, 8)
+    crp, cc, cv = bm.bcsr_to_csr(rp, c, v, 2)
+    A = bm.Matrix.from_csr(crp, cc, cv, len(crp) - 1)
+    for pre in ("none", "jacobi"):
+        x, info = bm.Solver(A, "fp64", preconditioner=pre).solve_host(rhs)
+        K = sp.csr_matrix((cv, cc, crp))
+        assert info["status"] == bm.SUCCESS
+        assert np.linalg.norm(rhs - K @ x) / np.linalg.norm(rhs) < 1e-10
+
+
+def test_fp32_solver_reaches_fp32_tolerance(lib, cuda):
+    rp, c, v = diag_dominant_bcsr(500, 2, seed=9)
+    K = bcsr_dense_csr(rp, c, v, 2)
+    b = np.random.default_rng(2).uniform(-1, 1, 1000)
+    A32 = bm.Matrix.from_bcsr(rp, c, v.astype(np.float32), 2)
+    x, info = bm.Solver(A32, "fp32", tol=1e-5).solve_host(b.astype(np.float32))
+    assert info["status"] == bm.SUCCESS and info["iterations_fp32"] == info["iterations"]
+    assert np.linalg.norm(b - K @ x.astype(np.float64)) / np.linalg.norm(b) < 1e-4
+
+
+def test_mixed_precision_refines_to_fp64_accuracy(lib, cuda):
+    rp, c, v = diag_dominant_bcsr(2000, 2, seed=4)
+    K = bcsr_dense_csr(rp, c, v, 2)
+    b = np.random.default_rng(3).uniform(-1, 1, 4000)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    x, info = bm.Solver(A, "mixed", tol=1e-10).solve_host(b)
+    assert info["status"] == bm.SUCCESS, info
+    assert info["used_fp64_fallback"] == 0 and info["iterations_fp32"] == info["iterations"]
+    assert info["refinements"] >= 2
+    assert np.linalg.norm(b - K @ x) / np.linalg.norm(b) < 1e-10
+    x64, i64 = bm.Solver(A, "fp64", tol=1e-10).solve_host(b)
+    assert np.linalg.norm(x - x64) / np.linalg.norm(x64) < 1e-9
+
+
+def test_mixed_precision_ill_conditioned_falls_back_and_converges(lib, cuda):
+    """cond(A) ~ 1e6 for a 100x25 Q4 grid: FP32 inner solves stall; the solver
+    finishes in FP64 and still meets the tolerance."""
+    rp, c, v, rhs = bm.gen_q4_elasticity(100, 25)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    x, info = bm.Solver(A, "mixed", tol=1e-10, max_iters=50000).solve_host(rhs)
+    K = bcsr_dense_csr(rp, c, v, 2)
+    assert info["status"] == bm.SUCCESS, info
+    assert np.linalg.norm(rhs - K @ x) / np.linalg.norm(rhs) < 1e-10
+
+
+def test_zero_rhs_and_iteration_limit(lib, cuda):
+    rp, c, v, rhs = bm.gen_q4_elasticity(30, 8)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    x, info = bm.Solver(A, "fp64").solve_host(np.zeros_like(rhs))
+    assert info["status"] == bm.SUCCESS and info["iterations"] == 0 and not x.any()
+    x, info = bm.Solver(A, "fp64", max_iters=5).solve_host(rhs)
+    assert info["status"] == bm.ERROR_NOT_CONVERGED and info["iterations"] == 5
+    assert np.isfinite(x).all() and x.any()
+
+
+def test_solver_rejects_bad_configurations(lib, cuda):
+    rp, c, v = bm.gen_band_bcsr(10, 3, 2, 2, seed=0)
+    A32 = bm.Matrix.from_bcsr(rp, c, v.astype(np.float32), 2)
+    with pytest.raises(bm.BmfpError):
+        bm.Solver(A32, "fp64")
+    with pytest.raises(bm.BmfpError):
+        bm.Solver(A32, "mixed")
+    rect = bm.Matrix.from_bcsr(rp, c, v, 2, n_block_cols=12)
+    with pytest.raises(bm.BmfpError):
+        bm.Solver(rect, "fp64")
