@@ -62,6 +62,9 @@ SIGNATURES = {
     "bmfp_solver_create": (c_int, [P(c_void_p), c_void_p, c_void_p, c_void_p]),
     "bmfp_solver_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "bmfp_solver_destroy": (c_int, [c_void_p]),
+    "bmfp_bicgstab_solve_noalloc": (c_int, [c_int, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p,
+                                            c_void_p, c_void_p, c_double, c_int, c_int, P(c_int),
+                                            P(c_double), c_void_p]),
     "bmfp_csr_spmv_bytes": (c_int64, [c_int, c_int, c_int, c_int64]),
 }
 

@@ -801,4 +801,90 @@ int WideEngine::true_residual (const void *d_b, void *d_r, double *rr, double *b
   *bb = b;
   return BMFP_SUCCESS;
 }
+// ------------------------------------------------------------ raw buffers
+// Launchers over caller-provided buffers, for the entry point that
+// allocates nothing (noalloc.cu). They run the same phase kernels as
+// WideEngine, without graphs.
+
+int raw_solve_grid (int64_t n, int *grid)
+{
+  int dev = 0, sms = 0;
+  BMFP_CUDA (cudaGetDevice (&dev));
+  BMFP_CUDA (cudaDeviceGetAttribute (&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int64_t want = std::max<int64_t> (1, (n + kThreads - 1) / kThreads);
+  *grid = (int) std::min<int64_t> ((int64_t) sms * 4, want);
+  return BMFP_SUCCESS;
+}
+
+namespace
+{
+int raw_kind (const RawSolve &b)
+{
+  const int kind = spmv_kind_for (&b.A);
+  if (b.aligned)
+    return kind;
+  // The vectorised row routine needs 16-byte aligned values; fall back to
+  // scalar loads for caller arrays that are not.
+  return (kind == kCsr8 || kind == kTpr3) ? kind : kTprAny;
+}
+
+template <typename T> Args<T> raw_args (const RawSolve &b)
+{
+  void *q = b.jacobi ? b.q : b.p;
+  void *z = b.jacobi ? b.z : b.s;
+  return make_args<T> (&b.A, b.n, b.x, b.r, b.rh, b.p, b.v, q, b.s, z, b.t, b.P, b.part, b.grid, b.st);
+}
+} // namespace
+
+int raw_jacobi (const RawSolve &b, cudaStream_t s)
+{
+  const int bs = b.A.bs ? b.A.bs : 1;
+  if (b.A.dtype == BMFP_R64F)
+    jacobi_kernel<double><<<b.grid, kThreads, 0, s>>> (b.A.n_rows, bs, b.A.d_row_ptr, b.A.d_cols,
+                                                       (const double *) b.A.d_vals, (double *) b.P);
+  else
+    jacobi_kernel<float><<<b.grid, kThreads, 0, s>>> (b.A.n_rows, bs, b.A.d_row_ptr, b.A.d_cols,
+                                                      (const float *) b.A.d_vals, (float *) b.P);
+  BMFP_LAUNCH_CHECK ();
+  return BMFP_SUCCESS;
+}
+
+int raw_start (const RawSolve &b, const void *d_rhs, double tol, int max_iter, cudaStream_t s)
+{
+  if (b.A.dtype == BMFP_R64F)
+    start_kernel<double, true><<<b.grid, kThreads, 0, s>>> (raw_args<double> (b), (const double *) d_rhs,
+                                                            tol, max_iter, -1.0);
+  else
+    start_kernel<float, true><<<b.grid, kThreads, 0, s>>> (raw_args<float> (b), (const float *) d_rhs,
+                                                           tol, max_iter, -1.0);
+  BMFP_LAUNCH_CHECK ();
+  return BMFP_SUCCESS;
+}
+
+int raw_phase (const RawSolve &b, int phase, cudaStream_t s)
+{
+  const int kind = raw_kind (b);
+  if (b.A.dtype == BMFP_R64F)
+    {
+      const Args<double> a = raw_args<double> (b);
+      if (phase == 2 || phase == 4)
+        launch_spmv_dispatch<double> (kind, phase, a, s);
+      else if (b.jacobi)
+        launch_vector_phase<double, true> (phase, a, s);
+      else
+        launch_vector_phase<double, false> (phase, a, s);
+    }
+  else
+    {
+      const Args<float> a = raw_args<float> (b);
+      if (phase == 2 || phase == 4)
+        launch_spmv_dispatch<float> (kind, phase, a, s);
+      else if (b.jacobi)
+        launch_vector_phase<float, true> (phase, a, s);
+      else
+        launch_vector_phase<float, false> (phase, a, s);
+    }
+  BMFP_LAUNCH_CHECK ();
+  return BMFP_SUCCESS;
+}
 } // namespace bmfp

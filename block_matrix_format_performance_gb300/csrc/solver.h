@@ -86,6 +86,29 @@ private:
   cudaEvent_t ev_[2] = { nullptr, nullptr };
 };
 
+// Caller-provided buffers for one solve (used by the entry point that
+// allocates nothing): a non-owning view of the matrix arrays plus every
+// Krylov vector, the partial sums and the scalar state.
+struct RawSolve
+{
+  bmfp_matrix_s A;     // view of the caller's device arrays (owns nothing)
+  int64_t n = 0;       // scalar rows
+  int grid = 0;        // CTAs of every phase kernel
+  bool jacobi = false;
+  bool aligned = true; // values 16-byte aligned: the vectorised SpMV may run
+  void *x = nullptr, *r = nullptr, *rh = nullptr, *p = nullptr, *v = nullptr;
+  void *q = nullptr, *s = nullptr, *z = nullptr, *t = nullptr, *P = nullptr;
+  double *part = nullptr; // kRawParts * grid doubles
+  DevState *st = nullptr;
+};
+constexpr int kRawParts = 7;
+
+// Grid of the phase kernels for n rows (the same rule as WideEngine).
+int raw_solve_grid (int64_t n, int *grid);
+int raw_jacobi (const RawSolve &b, cudaStream_t stream);
+int raw_start (const RawSolve &b, const void *d_rhs, double tol, int max_iter, cudaStream_t stream);
+int raw_phase (const RawSolve &b, int phase, cudaStream_t stream);
+
 // Elementwise helpers used by the refinement loop (vector_ops.cu).
 int axpy_scaled_convert (int dst_dtype, int src_dtype, int64_t n, double a, const void *src,
                          void *dst, cudaStream_t stream); // dst += a * src

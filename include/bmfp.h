@@ -269,6 +269,29 @@ BMFP_API int bmfp_solver_solve (bmfp_solver_t s, const void *d_b, void *d_x, bmf
                                 void *stream);
 BMFP_API int bmfp_solver_destroy (bmfp_solver_t s);
 
+/* BiCGStab that allocates nothing. No counterpart in the reference: it is
+ * for callers that cannot call cudaMalloc (a device-memory pool or budget
+ * that forbids more allocations, real-time loops that cannot take an
+ * allocation's implicit synchronisation, plug-ins whose host owns every
+ * allocation). The caller passes the matrix (BCSR with bs >= 1, or CSR with
+ * bs = 0 and n_block_rows = rows), b and x; every other vector lives in a
+ * fixed file-scope device array of about 9.5 MB that each GPU loading the
+ * library holds until exit. Limit: n_block_rows * max(bs,1) <= 131072 rows
+ * (larger systems get BMFP_ERROR_NOT_SUPPORTED; use bmfp_solver_create).
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture. All calls share the array: calls
+ * that overlap on the GPU (other threads or streams) race and must be
+ * serialised by the caller. Stops on the recursive residual
+ * ||r_i|| / ||b|| < tolerance (the reference's rule, gpu/bicgstab.cu:512);
+ * *iterations and *rel_residual (that recursive value) may be NULL. Blocks
+ * until the solve ends. */
+BMFP_API int bmfp_bicgstab_solve_noalloc (int dtype, int n_block_rows, int bs, int64_t nnzb,
+                                          const int *d_row_ptr, const int *d_cols,
+                                          const void *d_values, const void *d_b, void *d_x,
+                                          double tolerance, int max_iterations,
+                                          int preconditioner, int *iterations,
+                                          double *rel_residual, void *stream);
+
 /* --------------------------------------------------- host-side utilities ---
  * Pure host functions (no GPU needed). */
 
