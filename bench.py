@@ -69,8 +69,14 @@ def parse_args():
     ap.add_argument("--dtypes", default=",".join(DTYPES))
     ap.add_argument("--n-block-rows", type=int, default=NBR,
                     help="block rows per matrix (smaller only for profiling captures)")
-    ap.add_argument("--workload", choices=("spmv", "solve"), default="spmv",
-                    help="spmv: the block-size sweep line (default); solve: one Q4 elasticity solve")
+    ap.add_argument("--workload", choices=("spmv", "solve", "batch", "serve"), default="spmv",
+                    help="spmv: the block-size sweep line (default); solve: one Q4 elasticity solve; "
+                         "batch: 256 uneven Q4 systems in one persistent launch")
+    ap.add_argument("--systems", type=int, default=256, help="batch: number of systems")
+    ap.add_argument("--requests", type=int, default=1000, help="serve: number of requests")
+    ap.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (req/s)")
+    ap.add_argument("--baseline-requests", type=int, default=200,
+                    help="serve: requests of the same stream timed on the plain FP64 per-request solver")
     ap.add_argument("--grid", default="200x50", help="solve: nodes nx x ny of the Q4 grid")
     ap.add_argument("--precision", default="fp64", choices=("fp64", "fp32", "mixed"))
     ap.add_argument("--tol", type=float, default=1e-10)
@@ -483,10 +489,164 @@ def run_solve(args):
     A.close()
 
 
+def batch_grids(n_systems, seed=0):
+    """nx log-uniform in [20, 400] (seeded), ny = nx / 4: the uneven-batch workload."""
+    rng = np.random.default_rng(seed)
+    nxs = np.round(np.exp(rng.uniform(np.log(20), np.log(400), n_systems))).astype(int)
+    return [(int(nx), max(2, int(round(nx / 4)))) for nx in nxs]
+
+
+def run_batch(args):
+    """Uneven batch: every system solved by one persistent, graph-captured
+    launch (precision --precision), against the plain FP64 per-request solver
+    run system after system."""
+    import torch
+
+    import block_matrix_format_performance_gb300 as bm
+    from block_matrix_format_performance_gb300 import build as B
+    B.build()
+    grids = batch_grids(args.systems)
+    mats, rhs = [], []
+    for nx, ny in grids:
+        rp, c, v, b = bm.gen_q4_elasticity(nx, ny)
+        mats.append(bm.Matrix.from_bcsr(rp, c, v, 2))
+        rhs.append(b)
+    d_b = [torch.from_numpy(b).cuda() for b in rhs]
+    d_x = [torch.empty_like(b) for b in d_b]
+    batch = bm.Batch(mats, args.precision, tol=args.tol, max_iters=args.max_iters)
+    t0 = time.perf_counter()
+    cluster, threads = batch.autotune(d_b, d_x, probe_iterations=16)
+    tune_s = time.perf_counter() - t0
+    batch.solve(d_b, d_x)
+    times, infos = [], None
+    for _ in range(max(1, args.repeats)):
+        t0 = time.perf_counter()
+        infos = batch.solve(d_b, d_x)
+        times.append(time.perf_counter() - t0)
+    batch_s = min(times)
+    per_request_s = None
+    seq_infos = []
+    if args.repeats > 0:
+        t0 = time.perf_counter()
+        for m, b, x in zip(mats, d_b, d_x):
+            s = bm.Solver(m, "fp64", tol=args.tol, max_iters=args.max_iters)
+            seq_infos.append(s.solve(b, x))
+            s.close()
+        per_request_s = time.perf_counter() - t0
+    conv = sum(i["status"] == 0 for i in infos)
+    print(json.dumps({
+        "workload": "batch", "systems": len(grids), "dofs_total": int(sum(2 * a * b for a, b in grids)),
+        "precision": args.precision, "tol": args.tol, "cluster": cluster, "threads_per_cta": threads,
+        "autotune_s": round(tune_s, 3), "batch_s": round(batch_s, 4), "solves_per_s": round(len(grids) / batch_s, 2),
+        "converged": conv, "worst_true_rel": max(i["true_rel_residual"] for i in infos),
+        "iterations": sum(i["iterations"] for i in infos), "iterations_fp32": sum(i["iterations_fp32"] for i in infos),
+        "fp64_fallbacks": sum(i["used_fp64_fallback"] for i in infos),
+        "per_request_fp64_s": round(per_request_s, 4) if per_request_s else None,
+        "per_request_fp64_solves_per_s": round(len(grids) / per_request_s, 2) if per_request_s else None,
+        "per_request_fp64_converged": sum(i["status"] == 0 for i in seq_infos),
+        "not_converged": [{"grid": grids[k], "true_rel": i["true_rel_residual"]} for k, i in enumerate(infos)
+                          if i["status"] != 0][:20]}), flush=True)
+
+
+def serve_stream(n_requests, rate, seed=1):
+    """Seeded request stream: Poisson arrivals, grids as the uneven batch plus
+    5 % 1000 x 250, right-hand sides uniform in [-1, 1) (0 on clamped DOFs)."""
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_requests))
+    nxs = np.round(np.exp(rng.uniform(np.log(20), np.log(400), n_requests))).astype(int)
+    big = rng.random(n_requests) < 0.05
+    grids = [(1000, 250) if bg else (int(nx), max(2, int(round(nx / 4)))) for nx, bg in zip(nxs, big)]
+    return arrivals, grids
+
+
+def run_serve(args):
+    """Served solve stream through the continuous-batching server, and the
+    same stream's head on the plain FP64 per-request solver (FIFO)."""
+    import threading
+
+    import torch
+
+    import block_matrix_format_performance_gb300 as bm
+    from block_matrix_format_performance_gb300 import build as B
+    B.build()
+    arrivals, grids = serve_stream(args.requests, args.rate)
+    mats = {}
+    for g in sorted(set(grids)):
+        rp, c, v, _ = bm.gen_q4_elasticity(*g)
+        mats[g] = bm.Matrix.from_bcsr(rp, c, v, 2)
+    rng = np.random.default_rng(7)
+    rhs = []
+    for nx, ny in grids:
+        b = rng.uniform(-1, 1, 2 * nx * ny)
+        b.reshape(ny, nx, 2)[:, 0, :] = 0.0  # clamped column carries no load
+        rhs.append(b)
+    xs = [np.zeros_like(b) for b in rhs]
+    srv = bm.Server(args.precision, tol=args.tol, max_iters=args.max_iters)
+    # warm-up: one small request
+    w = np.zeros(mats[min(mats)].rows)
+    srv.wait(srv.submit(mats[min(mats)], np.ones_like(w), w))
+    tickets = [None] * len(grids)
+    t_start = time.perf_counter()
+
+    def producer():
+        for k, (t_arr, g) in enumerate(zip(arrivals, grids)):
+            delay = t_arr - (time.perf_counter() - t_start)
+            if delay > 0:
+                time.sleep(delay)
+            tickets[k] = srv.submit(mats[g], rhs[k], xs[k])
+
+    th = threading.Thread(target=producer)
+    th.start()
+    th.join()
+    infos = []
+    for t in tickets:
+        infos.append(srv.wait(t))
+    makespan = time.perf_counter() - t_start
+    stats = srv.stats()
+    srv.close()
+    lat = np.array([i["seconds"] for i in infos])
+    conv = sum(i["status"] == 0 for i in infos)
+    # baseline: plain FP64 per-request solver, FIFO on one GPU, same stream head
+    nb = min(args.baseline_requests, len(grids))
+    solvers = {}
+    service = []
+    for k in range(nb):
+        g = grids[k]
+        if g not in solvers:
+            solvers[g] = bm.Solver(mats[g], "fp64", tol=args.tol, max_iters=args.max_iters)
+        d_b = torch.from_numpy(rhs[k]).cuda()
+        d_x = torch.empty_like(d_b)
+        t0 = time.perf_counter()
+        solvers[g].solve(d_b, d_x)
+        service.append(time.perf_counter() - t0)
+    done, base_lat = 0.0, []
+    for k in range(nb):
+        done = max(done, arrivals[k]) + service[k]
+        base_lat.append(done - arrivals[k])
+    base_tput = nb / max(done, 1e-9)
+    print(json.dumps({
+        "workload": "serve", "requests": len(grids), "rate_req_s": args.rate, "precision": args.precision,
+        "tol": args.tol, "large_requests": int(sum(g == (1000, 250) for g in grids)),
+        "makespan_s": round(makespan, 3), "solves_per_s": round(len(grids) / makespan, 2),
+        "latency_p50_s": round(float(np.percentile(lat, 50)), 4), "latency_p99_s": round(float(np.percentile(lat, 99)), 4),
+        "converged": conv, "worst_true_rel": max(i["true_rel_residual"] for i in infos),
+        "micro_batches": stats["micro_batches"], "wide_solves": stats["wide_solves"],
+        "peak_device_bytes": stats["peak_bytes"],
+        "per_request_fp64": {"requests": nb, "solves_per_s": round(base_tput, 2),
+                             "latency_p50_s": round(float(np.percentile(base_lat, 50)), 4),
+                             "latency_p99_s": round(float(np.percentile(base_lat, 99)), 4)}}), flush=True)
+
+
 def main():
     args = parse_args()
+    if args.workload == "serve":
+        run_serve(args)
+        return
     if args.workload == "solve":
         run_solve(args)
+        return
+    if args.workload == "batch":
+        run_batch(args)
         return
     if args.impl == "reference":
         run_reference(args)

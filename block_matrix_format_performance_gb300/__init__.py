@@ -13,7 +13,8 @@ import ctypes
 
 import numpy as np
 
-from ._capi import BmfpError, SolveInfo, SolverOptions, check, load, LIB_PATH  # noqa: F401
+from ._capi import (BmfpError, ServerOptions, ServerStats, SolveInfo, SolverOptions, check, load,  # noqa: F401
+                    LIB_PATH)
 
 R32F, R64F = 0, 1
 
@@ -335,6 +336,112 @@ class Solver:
     def close(self):
         if getattr(self, "handle", None):
             load().bmfp_solver_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """bmfp_batch_t: many systems in one persistent, graph-captured launch."""
+
+    def __init__(self, matrices, precision="fp64", tol=1e-10, max_iters=100000, stream=None, **kw):
+        self.matrices = list(matrices)
+        self.options = solver_options(precision=precision, tolerance=tol, max_iterations=max_iters, **kw)
+        n = len(self.matrices)
+        arr = (ctypes.c_void_p * max(n, 1))(*[m.handle.value if hasattr(m.handle, "value") else m.handle
+                                               for m in self.matrices])
+        h = ctypes.c_void_p()
+        check(load().bmfp_batch_create(ctypes.byref(h), n, arr, ctypes.byref(self.options), _stream(stream)))
+        self.handle = h
+        self.n = n
+
+    def _ptrs(self, tensors):
+        return (ctypes.c_void_p * max(self.n, 1))(*[_p(t) for t in tensors])
+
+    def configure(self, cluster_size, threads_per_cta):
+        check(load().bmfp_batch_configure(self.handle, cluster_size, threads_per_cta))
+
+    def autotune(self, d_bs, d_xs, probe_iterations=16, stream=None):
+        c, t = ctypes.c_int(0), ctypes.c_int(0)
+        check(load().bmfp_batch_autotune(self.handle, self._ptrs(d_bs), self._ptrs(d_xs), probe_iterations,
+                                         ctypes.byref(c), ctypes.byref(t), _stream(stream)))
+        return c.value, t.value
+
+    def solve(self, d_bs, d_xs, stream=None):
+        infos = (SolveInfo * max(self.n, 1))()
+        st = load().bmfp_batch_solve(self.handle, self._ptrs(d_bs), self._ptrs(d_xs), infos, _stream(stream))
+        if st not in (SUCCESS, ERROR_NOT_CONVERGED, ERROR_BREAKDOWN):
+            check(st)
+        return [infos[i].as_dict() for i in range(self.n)]
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().bmfp_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """bmfp_server_t: continuous batching of solve requests."""
+
+    def __init__(self, precision="fp64", tol=1e-10, max_iters=100000, hbm_budget_bytes=120 << 30, **kw):
+        o = ServerOptions()
+        load().bmfp_server_options_init(ctypes.byref(o))
+        o.hbm_budget_bytes = hbm_budget_bytes
+        for k in ("max_in_flight", "max_batch", "streams", "cluster_size", "threads_per_cta", "wide_threshold_rows",
+                  "wide_lanes"):
+            if k in kw:
+                setattr(o, k, kw.pop(k))
+        o.solver = solver_options(precision=precision, tolerance=tol, max_iterations=max_iters, **kw)
+        self.options = o
+        h = ctypes.c_void_p()
+        check(load().bmfp_server_create(ctypes.byref(h), ctypes.byref(o)))
+        self.handle = h
+        self._keep = {}
+
+    def submit(self, matrix, b, x_out):
+        """Queue A x = b (host float64 arrays); x_out is filled on completion."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        t = ctypes.c_uint64(0)
+        check(load().bmfp_server_submit(self.handle, matrix.handle, _p(b), _p(x_out), ctypes.byref(t)))
+        self._keep[t.value] = (b, x_out)
+        return t.value
+
+    def poll(self, ticket):
+        info = SolveInfo()
+        st = load().bmfp_server_poll(self.handle, ticket, ctypes.byref(info))
+        if st == PENDING:
+            return None
+        if st not in (SUCCESS, ERROR_NOT_CONVERGED, ERROR_BREAKDOWN):
+            check(st)
+        self._keep.pop(ticket, None)
+        return info.as_dict()
+
+    def wait(self, ticket):
+        info = SolveInfo()
+        st = load().bmfp_server_wait(self.handle, ticket, ctypes.byref(info))
+        if st not in (SUCCESS, ERROR_NOT_CONVERGED, ERROR_BREAKDOWN):
+            check(st)
+        self._keep.pop(ticket, None)
+        return info.as_dict()
+
+    def stats(self):
+        s = ServerStats()
+        check(load().bmfp_server_get_stats(self.handle, ctypes.byref(s)))
+        return s.as_dict()
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().bmfp_server_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

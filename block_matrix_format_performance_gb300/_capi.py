@@ -62,6 +62,18 @@ SIGNATURES = {
     "bmfp_solver_create": (c_int, [P(c_void_p), c_void_p, c_void_p, c_void_p]),
     "bmfp_solver_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "bmfp_solver_destroy": (c_int, [c_void_p]),
+    "bmfp_batch_create": (c_int, [P(c_void_p), c_int, c_void_p, c_void_p, c_void_p]),
+    "bmfp_batch_configure": (c_int, [c_void_p, c_int, c_int]),
+    "bmfp_batch_autotune": (c_int, [c_void_p, c_void_p, c_void_p, c_int, P(c_int), P(c_int), c_void_p]),
+    "bmfp_batch_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "bmfp_batch_destroy": (c_int, [c_void_p]),
+    "bmfp_server_options_init": (None, [c_void_p]),
+    "bmfp_server_create": (c_int, [P(c_void_p), c_void_p]),
+    "bmfp_server_submit": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, P(c_uint64)]),
+    "bmfp_server_poll": (c_int, [c_void_p, c_uint64, c_void_p]),
+    "bmfp_server_wait": (c_int, [c_void_p, c_uint64, c_void_p]),
+    "bmfp_server_get_stats": (c_int, [c_void_p, c_void_p]),
+    "bmfp_server_destroy": (c_int, [c_void_p]),
     "bmfp_bicgstab_solve_noalloc": (c_int, [c_int, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p,
                                             c_void_p, c_void_p, c_double, c_int, c_int, P(c_int),
                                             P(c_double), c_void_p]),
@@ -82,6 +94,23 @@ class SolveInfo(ctypes.Structure):
     _fields_ = [("status", c_int), ("iterations", c_int), ("iterations_fp32", c_int), ("refinements", c_int),
                 ("restarts", c_int), ("used_fp64_fallback", c_int), ("true_rel_residual", c_double),
                 ("recursive_rel_residual", c_double), ("seconds", c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class ServerOptions(ctypes.Structure):
+    """struct bmfp_server_options (include/bmfp.h)."""
+    _fields_ = [("hbm_budget_bytes", ctypes.c_size_t), ("max_in_flight", c_int), ("max_batch", c_int),
+                ("streams", c_int), ("cluster_size", c_int), ("threads_per_cta", c_int),
+                ("wide_threshold_rows", c_int64), ("wide_lanes", c_int), ("solver", SolverOptions)]
+
+
+class ServerStats(ctypes.Structure):
+    """struct bmfp_server_stats (include/bmfp.h)."""
+    _fields_ = [("submitted", c_uint64), ("completed", c_uint64), ("micro_batches", c_uint64),
+                ("wide_solves", c_uint64), ("bytes_in_use", ctypes.c_size_t), ("peak_bytes", ctypes.c_size_t),
+                ("in_flight", c_int), ("pending", c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -1,0 +1,556 @@
+// Serving loop: continuous batching of solve requests on one GPU.
+//
+// Callers submit (matrix handle, right-hand side) requests from any thread;
+// a dispatcher thread admits them in arrival order while the device memory
+// they need fits the HBM budget and the in-flight limit, and launches what it
+// admitted right away as a micro-batch: one persistent cluster-per-system
+// launch of the batched BiCGStab kernel (batch.cu) on one of several streams.
+// Requests that arrive while earlier micro-batches are still running join the
+// GPU in their own launches, which overlap on the device with the running
+// ones; memory returns to the budget as each micro-batch completes. Matrices
+// stay resident (handles owned by the caller; FP32 copies for mixed
+// precision are made once per matrix and kept), and each request's Krylov
+// state lives on the device from admission to completion. Requests above
+// wide_threshold_rows go to whole-GPU lanes (the single-system engine), each
+// on its own thread and stream, several at once.
+//
+// A request's numbers do not depend on what else is in flight: the batched
+// kernel solves every system alone within its cluster, in a fixed reduction
+// order, and the micro-batch configuration (cluster size, CTA width) is fixed
+// per server.
+#include "batch.h"
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+using namespace bmfp;
+using Clock = std::chrono::steady_clock;
+
+namespace
+{
+struct Request
+{
+  uint64_t ticket = 0;
+  const bmfp_matrix_s *A = nullptr;
+  std::vector<double> b;
+  double *h_x = nullptr;
+  int64_t n = 0;
+  size_t bytes = 0;
+  Clock::time_point t_submit;
+  bmfp_solve_info info{};
+  bool done = false;
+  bool wide = false;
+  // device slices (inside the micro-batch's allocation)
+  double *d_b = nullptr, *d_x = nullptr, *w64 = nullptr;
+  float *w32 = nullptr;
+};
+
+struct MicroBatch
+{
+  std::vector<Request *> reqs;
+  int stream = 0;
+  void *d_mem = nullptr;
+  size_t bytes = 0;
+  BatchDesc *h_desc = nullptr; // pinned
+  BatchOut *h_out = nullptr;   // pinned
+  cudaEvent_t done = nullptr;
+};
+
+size_t align256 (size_t b) { return (b + 255) & ~(size_t) 255; }
+} // namespace
+
+struct bmfp_server_s
+{
+  bmfp_server_options opts{};
+  int device = 0;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Request *> pending;
+  std::deque<Request *> wide_queue;
+  std::unordered_map<uint64_t, std::unique_ptr<Request>> requests;
+  std::vector<std::unique_ptr<MicroBatch>> running;
+  std::map<const bmfp_matrix_s *, void *> vals32; // FP32 copies for mixed / FP32 serving
+  std::map<std::pair<int, const bmfp_matrix_s *>, bmfp_solver_t> wide_solvers; // per (lane, matrix)
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaStream_t> wide_streams;
+  size_t bytes_in_use = 0, peak_bytes = 0;
+  int in_flight = 0;
+  uint64_t next_ticket = 1, submitted = 0, completed = 0, micro_batches = 0, wide_solves = 0;
+  int op = -1;
+  int cluster_cap = 1;
+  bool stop = false;
+  int error = BMFP_SUCCESS;
+  std::thread dispatcher;
+  std::vector<std::thread> wide_workers;
+};
+
+namespace
+{
+size_t request_bytes (const bmfp_server_s *sv, int64_t n, bool wide)
+{
+  if (wide)
+    return (size_t) n * 8 * 14; // solver vectors (work and Krylov) + b, x
+  size_t b = align256 (n * 8) * 2 + align256 (n * 8 * 8); // b, x, 8 FP64 work vectors
+  if (sv->opts.solver.precision != BMFP_SOLVE_FP64)
+    b += align256 (n * 4 * 8); // 8 FP32 work vectors
+  return b;
+}
+
+int ensure_vals32 (bmfp_server_s *sv, const bmfp_matrix_s *A, cudaStream_t s)
+{
+  if (sv->opts.solver.precision == BMFP_SOLVE_FP64 || sv->vals32.count (A))
+    return BMFP_SUCCESS;
+  const int64_t nv = A->bs ? A->nnz * A->bs * A->bs : A->nnz;
+  void *p = nullptr;
+  BMFP_CUDA (cudaMalloc (&p, sizeof (float) * (size_t) std::max<int64_t> (nv, 1)));
+  int rc = convert_values (BMFP_R64F, BMFP_R32F, nv, A->d_vals, p, s);
+  if (rc == BMFP_SUCCESS && cudaStreamSynchronize (s) != cudaSuccess)
+    rc = BMFP_ERROR_CUDA; // other streams read the copy next
+  if (rc != BMFP_SUCCESS)
+    {
+      cudaFree (p);
+      return rc;
+    }
+  sv->vals32[A] = p;
+  sv->bytes_in_use += sizeof (float) * (size_t) nv;
+  return BMFP_SUCCESS;
+}
+
+void finish (bmfp_server_s *sv, Request *r)
+{
+  r->info.seconds = std::chrono::duration<double> (Clock::now () - r->t_submit).count ();
+  r->done = true;
+  sv->completed++;
+}
+
+// Launch one micro-batch (called with the lock held; the device work is
+// asynchronous on the chosen stream).
+int launch_micro_batch (bmfp_server_s *sv, std::vector<Request *> &reqs)
+{
+  std::unique_ptr<MicroBatch> mb (new MicroBatch);
+  mb->reqs = reqs;
+  mb->stream = (int) (sv->micro_batches % sv->streams.size ());
+  cudaStream_t s = sv->streams[mb->stream];
+  const int n = (int) reqs.size ();
+  size_t total = align256 (sizeof (BatchDesc) * n) + align256 (sizeof (BatchOut) * n) + 256 + align256 (sizeof (int) * n);
+  for (Request *r : reqs)
+    total += r->bytes;
+  BMFP_CUDA (cudaMallocAsync (&mb->d_mem, total, s));
+  mb->bytes = total;
+  BMFP_CUDA (cudaMallocHost (&mb->h_desc, sizeof (BatchDesc) * n));
+  BMFP_CUDA (cudaMallocHost (&mb->h_out, sizeof (BatchOut) * n));
+  char *p = (char *) mb->d_mem;
+  BatchDesc *d_desc = (BatchDesc *) p;
+  p += align256 (sizeof (BatchDesc) * n);
+  BatchOut *d_out = (BatchOut *) p;
+  p += align256 (sizeof (BatchOut) * n);
+  int *d_counter = (int *) p;
+  p += 256;
+  int *d_order = (int *) p;
+  p += align256 (sizeof (int) * n);
+  std::vector<int> order (n);
+  for (int i = 0; i < n; i++)
+    {
+      Request *r = reqs[i];
+      r->d_b = (double *) p;
+      p += align256 (r->n * 8);
+      r->d_x = (double *) p;
+      p += align256 (r->n * 8);
+      r->w64 = (double *) p;
+      p += align256 (r->n * 8 * 8);
+      if (sv->opts.solver.precision != BMFP_SOLVE_FP64)
+        {
+          r->w32 = (float *) p;
+          p += align256 (r->n * 4 * 8);
+        }
+      BMFP_CUDA (cudaMemcpyAsync (r->d_b, r->b.data (), sizeof (double) * r->n, cudaMemcpyHostToDevice, s));
+      BatchDesc &D = mb->h_desc[i];
+      const bmfp_matrix_s *A = r->A;
+      D.nbr = A->n_rows;
+      D.bs = A->bs ? A->bs : 1;
+      D.op = sv->op;
+      D.n = r->n;
+      D.rp = A->d_row_ptr;
+      D.cols = A->d_cols;
+      D.vals64 = (const double *) A->d_vals;
+      D.vals32 = sv->opts.solver.precision != BMFP_SOLVE_FP64 ? (const float *) sv->vals32[A] : nullptr;
+      D.b = r->d_b;
+      D.x = r->d_x;
+      D.w64 = r->w64;
+      D.w32 = r->w32;
+      order[i] = i;
+    }
+  std::stable_sort (order.begin (), order.end (), [&] (int a, int b) { return reqs[a]->n > reqs[b]->n; });
+  BMFP_CUDA (cudaMemcpyAsync (d_desc, mb->h_desc, sizeof (BatchDesc) * n, cudaMemcpyHostToDevice, s));
+  BMFP_CUDA (cudaMemcpyAsync (d_order, order.data (), sizeof (int) * n, cudaMemcpyHostToDevice, s));
+  BMFP_CUDA (cudaMemsetAsync (d_counter, 0, sizeof (int), s));
+  BatchParams P;
+  P.n_systems = n;
+  P.desc = d_desc;
+  P.out = d_out;
+  P.counter = d_counter;
+  P.order = d_order;
+  const bmfp_solver_options &o = sv->opts.solver;
+  P.precision = o.precision;
+  P.tol = o.tolerance;
+  P.max_it = o.max_iterations;
+  P.inner_tol = o.inner_tolerance;
+  P.inner_max = o.inner_max_iterations;
+  P.max_ref = o.max_refinements;
+  P.fallback = o.fallback_fp64;
+  const int clusters = std::max (1, std::min (n, sv->cluster_cap));
+  int rc = batch_launch (o.precision, sv->op, P, sv->opts.cluster_size, sv->opts.threads_per_cta,
+                         clusters * sv->opts.cluster_size, s);
+  if (rc != BMFP_SUCCESS)
+    return rc;
+  BMFP_CUDA (cudaMemcpyAsync (mb->h_out, d_out, sizeof (BatchOut) * n, cudaMemcpyDeviceToHost, s));
+  BMFP_CUDA (cudaEventCreateWithFlags (&mb->done, cudaEventDisableTiming));
+  BMFP_CUDA (cudaEventRecord (mb->done, s));
+  for (Request *r : reqs)
+    r->info.status = BMFP_PENDING;
+  sv->micro_batches++;
+  sv->running.push_back (std::move (mb));
+  return BMFP_SUCCESS;
+}
+
+// Retire completed micro-batches (lock held). Returns true if any finished.
+bool retire (bmfp_server_s *sv)
+{
+  bool any = false;
+  for (size_t k = 0; k < sv->running.size ();)
+    {
+      MicroBatch *mb = sv->running[k].get ();
+      const cudaError_t q = cudaEventQuery (mb->done);
+      if (q == cudaErrorNotReady)
+        {
+          k++;
+          continue;
+        }
+      if (q != cudaSuccess && sv->error == BMFP_SUCCESS)
+        sv->error = cuda_fail (q, "micro-batch", __FILE__, __LINE__);
+      for (size_t i = 0; i < mb->reqs.size (); i++)
+        {
+          Request *r = mb->reqs[i];
+          const BatchOut &o = mb->h_out[i];
+          if (q == cudaSuccess && r->h_x)
+            cudaMemcpy (r->h_x, r->d_x, sizeof (double) * r->n, cudaMemcpyDeviceToHost);
+          bmfp_solve_info &f = r->info;
+          f.status = q != cudaSuccess ? BMFP_ERROR_CUDA
+                                      : (o.status == 1 ? BMFP_SUCCESS
+                                                       : (o.status == 3 ? BMFP_ERROR_BREAKDOWN : BMFP_ERROR_NOT_CONVERGED));
+          f.iterations = o.iterations;
+          f.iterations_fp32 = o.iterations_fp32;
+          f.refinements = o.refinements;
+          f.restarts = o.restarts;
+          f.used_fp64_fallback = o.fallback;
+          f.true_rel_residual = o.true_rel;
+          f.recursive_rel_residual = o.rec_rel;
+          sv->bytes_in_use -= r->bytes;
+          sv->in_flight--;
+          finish (sv, r);
+        }
+      cudaFreeAsync (mb->d_mem, sv->streams[mb->stream]);
+      cudaEventDestroy (mb->done);
+      cudaFreeHost (mb->h_desc);
+      cudaFreeHost (mb->h_out);
+      sv->running.erase (sv->running.begin () + k);
+      any = true;
+    }
+  return any;
+}
+
+void dispatcher_main (bmfp_server_s *sv)
+{
+  cudaSetDevice (sv->device);
+  std::unique_lock<std::mutex> lk (sv->mu);
+  for (;;)
+    {
+      if (retire (sv))
+        sv->cv_done.notify_all ();
+      // Admit in arrival order while budget and slots allow.
+      std::vector<Request *> admitted;
+      while (!sv->pending.empty ())
+        {
+          Request *r = sv->pending.front ();
+          if (sv->bytes_in_use + r->bytes > sv->opts.hbm_budget_bytes || sv->in_flight >= sv->opts.max_in_flight)
+            break;
+          if (!r->wide && ensure_vals32 (sv, r->A, sv->streams[0]) != BMFP_SUCCESS)
+            break;
+          sv->pending.pop_front ();
+          sv->bytes_in_use += r->bytes;
+          sv->peak_bytes = std::max (sv->peak_bytes, sv->bytes_in_use);
+          sv->in_flight++;
+          if (r->wide)
+            {
+              sv->wide_queue.push_back (r);
+              sv->cv_work.notify_all ();
+              continue;
+            }
+          admitted.push_back (r);
+          if ((int) admitted.size () >= sv->opts.max_batch)
+            {
+              if (launch_micro_batch (sv, admitted) != BMFP_SUCCESS && sv->error == BMFP_SUCCESS)
+                sv->error = BMFP_ERROR_CUDA;
+              admitted.clear ();
+            }
+        }
+      if (!admitted.empty () && launch_micro_batch (sv, admitted) != BMFP_SUCCESS && sv->error == BMFP_SUCCESS)
+        sv->error = BMFP_ERROR_CUDA;
+      if (sv->stop && sv->pending.empty () && sv->running.empty () && sv->in_flight == 0)
+        break;
+      // Sleep until new work arrives or a short poll interval passes while
+      // micro-batches run (completion is polled through their events).
+      if (sv->running.empty () && sv->pending.empty () && !sv->stop)
+        sv->cv_work.wait (lk);
+      else
+        sv->cv_work.wait_for (lk, std::chrono::microseconds (50));
+    }
+}
+
+void wide_main (bmfp_server_s *sv, int lane)
+{
+  cudaSetDevice (sv->device);
+  cudaStream_t stream = sv->wide_streams[lane];
+  std::unique_lock<std::mutex> lk (sv->mu);
+  for (;;)
+    {
+      sv->cv_work.wait (lk, [&] { return !sv->wide_queue.empty () || (sv->stop && sv->pending.empty () && sv->in_flight == 0); });
+      if (sv->wide_queue.empty ())
+        break;
+      Request *r = sv->wide_queue.front ();
+      sv->wide_queue.pop_front ();
+      bmfp_solver_t solver = nullptr;
+      const auto key = std::make_pair (lane, r->A);
+      auto it = sv->wide_solvers.find (key);
+      int rc = BMFP_SUCCESS;
+      if (it == sv->wide_solvers.end ())
+        {
+          bmfp_solver_options o = sv->opts.solver;
+          rc = bmfp_solver_create (&solver, const_cast<bmfp_matrix_s *> (r->A), &o, stream);
+          if (rc == BMFP_SUCCESS)
+            sv->wide_solvers[key] = solver;
+        }
+      else
+        solver = it->second;
+      lk.unlock ();
+      double *d_b = nullptr, *d_x = nullptr;
+      if (rc == BMFP_SUCCESS && (cudaMalloc (&d_b, sizeof (double) * r->n) != cudaSuccess
+                                 || cudaMalloc (&d_x, sizeof (double) * r->n) != cudaSuccess))
+        rc = BMFP_ERROR_OUT_OF_MEMORY;
+      if (rc == BMFP_SUCCESS)
+        {
+          cudaMemcpyAsync (d_b, r->b.data (), sizeof (double) * r->n, cudaMemcpyHostToDevice, stream);
+          rc = bmfp_solver_solve (solver, d_b, d_x, &r->info, stream);
+          if (r->h_x)
+            cudaMemcpy (r->h_x, d_x, sizeof (double) * r->n, cudaMemcpyDeviceToHost);
+        }
+      else
+        r->info.status = rc;
+      cudaFree (d_b);
+      cudaFree (d_x);
+      lk.lock ();
+      sv->bytes_in_use -= r->bytes;
+      sv->in_flight--;
+      sv->wide_solves++;
+      finish (sv, r);
+      sv->cv_done.notify_all ();
+      sv->cv_work.notify_all ();
+    }
+}
+} // namespace
+
+extern "C" {
+
+void bmfp_server_options_init (bmfp_server_options *o)
+{
+  if (!o)
+    return;
+  o->hbm_budget_bytes = (size_t) 120 << 30;
+  o->max_in_flight = 4096;
+  o->max_batch = 64;
+  o->streams = 8;
+  o->cluster_size = 4;
+  o->threads_per_cta = 256;
+  o->wide_threshold_rows = 200000;
+  o->wide_lanes = 4;
+  bmfp_solver_options_init (&o->solver);
+}
+
+int bmfp_server_create (bmfp_server_t *out, const bmfp_server_options *opts)
+{
+  if (!out)
+    return fail (BMFP_ERROR_INVALID_VALUE, "null output");
+  *out = nullptr;
+  bmfp_server_options o;
+  bmfp_server_options_init (&o);
+  if (opts)
+    o = *opts;
+  if (o.max_in_flight < 1 || o.max_batch < 1 || o.streams < 1 || o.streams > 64 || o.hbm_budget_bytes == 0
+      || o.wide_lanes < 1 || o.wide_lanes > 16)
+    return fail (BMFP_ERROR_INVALID_VALUE, "invalid server options");
+  if (o.solver.preconditioner != BMFP_PRECOND_NONE)
+    return fail (BMFP_ERROR_NOT_SUPPORTED, "the server takes no preconditioner");
+  std::unique_ptr<bmfp_server_s> sv (new (std::nothrow) bmfp_server_s);
+  if (!sv)
+    return fail (BMFP_ERROR_OUT_OF_MEMORY, "host allocation failed");
+  sv->opts = o;
+  BMFP_CUDA (cudaGetDevice (&sv->device));
+  sv->streams.resize (o.streams);
+  for (auto &s : sv->streams)
+    BMFP_CUDA (cudaStreamCreateWithFlags (&s, cudaStreamNonBlocking));
+  sv->wide_streams.resize (o.wide_lanes);
+  for (auto &s : sv->wide_streams)
+    BMFP_CUDA (cudaStreamCreateWithFlags (&s, cudaStreamNonBlocking));
+  // Several micro-batches should run side by side: give each at most a
+  // quarter of the co-resident clusters.
+  int clusters = 0;
+  for (int op = 0; op < 3; op++)
+    {
+      int c = 0;
+      const int rc = batch_max_clusters (o.solver.precision, op, o.cluster_size, o.threads_per_cta, &c);
+      if (rc != BMFP_SUCCESS)
+        return rc;
+      clusters = op == 0 ? c : std::min (clusters, c);
+    }
+  if (clusters < 1)
+    return fail (BMFP_ERROR_NOT_SUPPORTED, "cluster %d x %d threads does not fit", o.cluster_size, o.threads_per_cta);
+  sv->cluster_cap = std::max (1, clusters / 4);
+  bmfp_server_s *raw = sv.get ();
+  raw->dispatcher = std::thread (dispatcher_main, raw);
+  for (int lane = 0; lane < o.wide_lanes; lane++)
+    raw->wide_workers.emplace_back (wide_main, raw, lane);
+  *out = sv.release ();
+  return BMFP_SUCCESS;
+}
+
+int bmfp_server_submit (bmfp_server_t sv, bmfp_matrix_t A, const double *h_b, double *h_x, uint64_t *ticket)
+{
+  if (!sv || !A || !h_b || !ticket)
+    return fail (BMFP_ERROR_INVALID_VALUE, "null argument");
+  if (A->dtype != BMFP_R64F || A->n_rows != A->n_cols || (A->bs ? A->bs : 1) > 32)
+    return fail (BMFP_ERROR_INVALID_VALUE, "requests need a square FP64 matrix with bs <= 32");
+  std::unique_ptr<Request> r (new (std::nothrow) Request);
+  if (!r)
+    return fail (BMFP_ERROR_OUT_OF_MEMORY, "host allocation failed");
+  r->A = A;
+  r->n = (int64_t) A->n_rows * (A->bs ? A->bs : 1);
+  r->b.assign (h_b, h_b + r->n);
+  r->h_x = h_x;
+  r->wide = r->n > sv->opts.wide_threshold_rows;
+  r->bytes = request_bytes (sv, r->n, r->wide);
+  r->t_submit = Clock::now ();
+  r->info.status = BMFP_PENDING;
+  if (r->bytes > sv->opts.hbm_budget_bytes)
+    return fail (BMFP_ERROR_BUDGET, "request needs %zu bytes, above the %zu-byte HBM budget", r->bytes,
+                 sv->opts.hbm_budget_bytes);
+  std::lock_guard<std::mutex> lk (sv->mu);
+  if (sv->error != BMFP_SUCCESS)
+    return fail (sv->error, "server stopped after an error");
+  const int op = batch_op_for (A);
+  if (!r->wide)
+    {
+      if (sv->op < 0)
+        sv->op = op;
+      else if (sv->op != op)
+        sv->op = 2; // mixed block sizes: the generic row routine serves all
+    }
+  r->ticket = sv->next_ticket++;
+  *ticket = r->ticket;
+  sv->pending.push_back (r.get ());
+  sv->requests[r->ticket] = std::move (r);
+  sv->submitted++;
+  sv->cv_work.notify_all ();
+  return BMFP_SUCCESS;
+}
+
+static int take_result (bmfp_server_t sv, uint64_t ticket, bmfp_solve_info *info, bool block)
+{
+  std::unique_lock<std::mutex> lk (sv->mu);
+  auto it = sv->requests.find (ticket);
+  if (it == sv->requests.end ())
+    return fail (BMFP_ERROR_INVALID_VALUE, "unknown ticket %llu", (unsigned long long) ticket);
+  if (block)
+    sv->cv_done.wait (lk, [&] { return it->second->done || sv->error != BMFP_SUCCESS; });
+  if (!it->second->done)
+    return sv->error != BMFP_SUCCESS ? sv->error : BMFP_PENDING;
+  if (info)
+    *info = it->second->info;
+  const int st = it->second->info.status;
+  sv->requests.erase (it);
+  return st;
+}
+
+int bmfp_server_poll (bmfp_server_t sv, uint64_t ticket, bmfp_solve_info *info)
+{
+  if (!sv)
+    return fail (BMFP_ERROR_INVALID_VALUE, "null server");
+  return take_result (sv, ticket, info, false);
+}
+
+int bmfp_server_wait (bmfp_server_t sv, uint64_t ticket, bmfp_solve_info *info)
+{
+  if (!sv)
+    return fail (BMFP_ERROR_INVALID_VALUE, "null server");
+  return take_result (sv, ticket, info, true);
+}
+
+int bmfp_server_get_stats (bmfp_server_t sv, bmfp_server_stats *st)
+{
+  if (!sv || !st)
+    return fail (BMFP_ERROR_INVALID_VALUE, "null argument");
+  std::lock_guard<std::mutex> lk (sv->mu);
+  st->submitted = sv->submitted;
+  st->completed = sv->completed;
+  st->micro_batches = sv->micro_batches;
+  st->wide_solves = sv->wide_solves;
+  st->bytes_in_use = sv->bytes_in_use;
+  st->peak_bytes = sv->peak_bytes;
+  st->in_flight = sv->in_flight;
+  st->pending = (int) sv->pending.size ();
+  return BMFP_SUCCESS;
+}
+
+int bmfp_server_destroy (bmfp_server_t sv)
+{
+  if (!sv)
+    return BMFP_SUCCESS;
+  {
+    std::lock_guard<std::mutex> lk (sv->mu);
+    sv->stop = true;
+    sv->cv_work.notify_all ();
+  }
+  if (sv->dispatcher.joinable ())
+    sv->dispatcher.join ();
+  {
+    std::lock_guard<std::mutex> lk (sv->mu);
+    sv->cv_work.notify_all ();
+  }
+  for (auto &t : sv->wide_workers)
+    if (t.joinable ())
+      t.join ();
+  for (auto &kv : sv->wide_solvers)
+    bmfp_solver_destroy (kv.second);
+  for (auto &kv : sv->vals32)
+    cudaFree (kv.second);
+  for (auto s : sv->streams)
+    {
+      cudaStreamSynchronize (s);
+      cudaStreamDestroy (s);
+    }
+  for (auto s : sv->wide_streams)
+    cudaStreamDestroy (s);
+  delete sv;
+  return BMFP_SUCCESS;
+}
+
+} // extern "C"

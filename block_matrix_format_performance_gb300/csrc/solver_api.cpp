@@ -1,5 +1,6 @@
 // C ABI of the BiCGStab solver: plain FP64 / FP32 solves and the mixed
 // FP32-inner / FP64-refinement driver, on top of WideEngine (bicgstab.cu).
+#include "batch.h"
 #include "solver.h"
 
 #include <chrono>
@@ -18,6 +19,7 @@ struct bmfp_solver_s
   std::unique_ptr<WideEngine> inner;    // FP32 engine (MIXED, or FP32 on an FP64 matrix)
   void *work_a = nullptr;               // residual / converted right-hand side
   void *work_b = nullptr;
+  void *work_c = nullptr;               // best iterate kept across restarts
 
   ~bmfp_solver_s ()
   {
@@ -27,6 +29,7 @@ struct bmfp_solver_s
       bmfp_matrix_destroy (A_owned);
     cudaFree (work_a);
     cudaFree (work_b);
+    cudaFree (work_c);
   }
 };
 
@@ -41,9 +44,59 @@ int status_of (const DevState &st)
   return BMFP_ERROR_NOT_CONVERGED;
 }
 
+// Restart loop shared by the plain and the mixed solves: verify b - A x,
+// restart from the true residual while each restart still lowers it (at most
+// 8 times), and keep the best iterate: near the attainable accuracy of the working
+// precision a restart can leave x worse (asking the recursive residual for
+// less than the tolerance only makes that more likely, measured), and then x
+// is restored.
+int finish_with_restarts (WideEngine &e, const void *d_b, void *d_r, void *d_xbest, const bmfp_solver_options &o,
+                          DevState &st, int iter_budget, double norm_b, int *restarts_out, double *rel_out,
+                          cudaStream_t s)
+{
+  const size_t xbytes = dtype_size (e.dtype ()) * (size_t) e.n ();
+  double best = INFINITY;
+  int restarts = 0;
+  DevState best_st = st;
+  for (;;)
+    {
+      double rr = 0, bb = 0;
+      int rc = e.true_residual (d_b, d_r, &rr, &bb, s);
+      if (rc != BMFP_SUCCESS)
+        return rc;
+      const double rel = bb > 0 ? std::sqrt (rr / bb) : 0.0;
+      if (!(rel < best))
+        {
+          if (restarts > 0)
+            {
+              BMFP_CUDA (cudaMemcpyAsync (e.x (), d_xbest, xbytes, cudaMemcpyDeviceToDevice, s));
+              BMFP_CUDA (cudaStreamSynchronize (s));
+              st = best_st;
+            }
+          else
+            best = rel;
+          break;
+        }
+      best = rel;
+      best_st = st;
+      if (rel < o.tolerance || st.status != kStateConverged || st.iter >= iter_budget || restarts >= 8)
+        break;
+      BMFP_CUDA (cudaMemcpyAsync (d_xbest, e.x (), xbytes, cudaMemcpyDeviceToDevice, s));
+      restarts++;
+      rc = e.start_residual (d_r, o.tolerance, iter_budget, norm_b > 0 ? norm_b : std::sqrt (bb), s);
+      if (rc == BMFP_SUCCESS)
+        rc = e.run (s, &st);
+      if (rc != BMFP_SUCCESS)
+        return rc;
+    }
+  *restarts_out = restarts;
+  *rel_out = best;
+  return BMFP_SUCCESS;
+}
+
 // Solve with one engine from x0 = 0, then (optionally) verify the true
-// residual and restart from it while the recursive residual stopped early.
-int solve_plain (WideEngine &e, const void *d_b, void *d_r, const bmfp_solver_options &o,
+// residual and restart from it (finish_with_restarts).
+int solve_plain (WideEngine &e, const void *d_b, void *d_r, void *d_xbest, const bmfp_solver_options &o,
                  bmfp_solve_info *info, cudaStream_t s)
 {
   DevState st{};
@@ -53,36 +106,16 @@ int solve_plain (WideEngine &e, const void *d_b, void *d_r, const bmfp_solver_op
   if (rc != BMFP_SUCCESS)
     return rc;
   int status = status_of (st);
-  double rel_true = NAN, prev_rel = INFINITY;
+  double rel_true = NAN;
   int restarts = 0;
   if (o.check_true_residual)
-    for (;;)
-      {
-        double rr = 0, bb = 0;
-        rc = e.true_residual (d_b, d_r, &rr, &bb, s);
-        if (rc != BMFP_SUCCESS)
-          return rc;
-        rel_true = bb > 0 ? std::sqrt (rr / bb) : 0.0;
-        if (rel_true < o.tolerance)
-          {
-            status = BMFP_SUCCESS;
-            break;
-          }
-        status = st.status == kStateBreakdown ? BMFP_ERROR_BREAKDOWN : BMFP_ERROR_NOT_CONVERGED;
-        // Restart from the true residual while that still gains accuracy; a
-        // restart that does not halve it means the attainable accuracy of the
-        // working precision has been reached.
-        if (st.status != kStateConverged || st.iter >= o.max_iterations || restarts >= 8
-            || !(rel_true < 0.5 * prev_rel))
-          break;
-        prev_rel = rel_true;
-        restarts++;
-        rc = e.start_residual (d_r, o.tolerance, o.max_iterations, -1.0, s);
-        if (rc == BMFP_SUCCESS)
-          rc = e.run (s, &st);
-        if (rc != BMFP_SUCCESS)
-          return rc;
-      }
+    {
+      rc = finish_with_restarts (e, d_b, d_r, d_xbest, o, st, o.max_iterations, -1.0, &restarts, &rel_true, s);
+      if (rc != BMFP_SUCCESS)
+        return rc;
+      status = rel_true < o.tolerance ? BMFP_SUCCESS
+                                      : (st.status == kStateBreakdown ? BMFP_ERROR_BREAKDOWN : BMFP_ERROR_NOT_CONVERGED);
+    }
   info->status = status;
   info->iterations += st.iter;
   info->restarts += restarts;
@@ -133,34 +166,18 @@ int solve_mixed (bmfp_solver_s *sv, const void *d_b, bmfp_solve_info *info, cuda
             rc = e64.run (s, &st);
           if (rc != BMFP_SUCCESS)
             return rc;
-          iters64 = st.iter;
           int restarts = 0;
-          double last = INFINITY;
-          for (;;)
-            {
-              rc = e64.true_residual (d_b, r64, &rr, &bb, s);
-              if (rc != BMFP_SUCCESS)
-                return rc;
-              info->true_rel_residual = bb > 0 ? std::sqrt (rr / bb) : 0.0;
-              info->recursive_rel_residual = st.norm_b > 0 ? std::sqrt (st.rr) / st.norm_b : 0.0;
-              if (info->true_rel_residual < o.tolerance)
-                {
-                  info->status = BMFP_SUCCESS;
-                  break;
-                }
-              info->status = st.status == kStateBreakdown ? BMFP_ERROR_BREAKDOWN : BMFP_ERROR_NOT_CONVERGED;
-              if (st.status != kStateConverged || restarts >= 8 || iters64 + iters32 >= o.max_iterations
-                  || !(info->true_rel_residual < 0.5 * last))
-                break;
-              last = info->true_rel_residual;
-              restarts++;
-              rc = e64.start_residual (r64, o.tolerance, o.max_iterations - iters32, -1.0, s);
-              if (rc == BMFP_SUCCESS)
-                rc = e64.run (s, &st);
-              if (rc != BMFP_SUCCESS)
-                return rc;
-              iters64 = st.iter;
-            }
+          double rel_fin = NAN;
+          rc = finish_with_restarts (e64, d_b, r64, sv->work_c, o, st, o.max_iterations - iters32, std::sqrt (bb),
+                                     &restarts, &rel_fin, s);
+          if (rc != BMFP_SUCCESS)
+            return rc;
+          iters64 = st.iter;
+          info->true_rel_residual = rel_fin;
+          info->recursive_rel_residual = st.norm_b > 0 ? std::sqrt (st.rr) / st.norm_b : 0.0;
+          info->status = rel_fin < o.tolerance ? BMFP_SUCCESS
+                                               : (st.status == kStateBreakdown ? BMFP_ERROR_BREAKDOWN
+                                                                               : BMFP_ERROR_NOT_CONVERGED);
           info->restarts += restarts;
           break;
         }
@@ -179,10 +196,10 @@ int solve_mixed (bmfp_solver_s *sv, const void *d_b, bmfp_solve_info *info, cuda
         return rc;
       iters32 += st.iter;
       info->refinements = k + 1;
-      if (st.status == kStateBreakdown && !(st.norm_b > 0 && std::sqrt (st.rr) < 0.5 * st.norm_b))
+      if (!(st.norm_b > 0 && std::sqrt (st.rr) < 0.5 * st.norm_b))
         {
-          // The FP32 inner solve broke down without halving its residual: do
-          // not apply it; the next pass falls back to FP64.
+          // The FP32 inner solve did not halve its residual (stagnation,
+          // breakdown or blow-up): do not apply it; fall back to FP64 next.
           prev_rel = 0.0;
           continue;
         }
@@ -274,6 +291,7 @@ int bmfp_solver_create (bmfp_solver_t *out, bmfp_matrix_t A, const bmfp_solver_o
   const size_t nb = (size_t) std::max (n_rows, 1);
   BMFP_CUDA (cudaMalloc (&sv->work_a, nb * 8));
   BMFP_CUDA (cudaMalloc (&sv->work_b, nb * 8));
+  BMFP_CUDA (cudaMalloc (&sv->work_c, nb * 8));
   *out = sv.release ();
   return BMFP_SUCCESS;
 }
@@ -305,7 +323,7 @@ int bmfp_solver_solve (bmfp_solver_t sv, const void *d_b, void *d_x, bmfp_solve_
           b = sv->work_b;
         }
       if (rc == BMFP_SUCCESS)
-        rc = solve_plain (e, b, sv->work_a, sv->opts, &info, s);
+        rc = solve_plain (e, b, sv->work_a, sv->work_c, sv->opts, &info, s);
       if (e.dtype () == BMFP_R32F)
         info.iterations_fp32 = info.iterations;
       if (rc == BMFP_SUCCESS)
@@ -331,6 +349,82 @@ int bmfp_solver_solve (bmfp_solver_t sv, const void *d_b, void *d_x, bmfp_solve_
 int bmfp_solver_destroy (bmfp_solver_t sv)
 {
   delete sv;
+  return BMFP_SUCCESS;
+}
+
+} // extern "C"
+
+struct bmfp_batch_s
+{
+  bmfp::BatchEngine engine;
+  int n = 0;
+};
+
+extern "C" {
+
+int bmfp_batch_create (bmfp_batch_t *out, int n, const bmfp_matrix_t *mats, const bmfp_solver_options *opts,
+                       void *stream)
+{
+  if (!out || n < 0 || (n > 0 && !mats))
+    return fail (BMFP_ERROR_INVALID_VALUE, "invalid arguments");
+  *out = nullptr;
+  bmfp_solver_options o;
+  bmfp_solver_options_init (&o);
+  if (opts)
+    o = *opts;
+  if (o.precision < BMFP_SOLVE_FP64 || o.precision > BMFP_SOLVE_MIXED || !(o.tolerance > 0))
+    return fail (BMFP_ERROR_INVALID_VALUE, "invalid precision or tolerance");
+  if (o.preconditioner != BMFP_PRECOND_NONE)
+    return fail (BMFP_ERROR_NOT_SUPPORTED, "batched solves take no preconditioner");
+  std::unique_ptr<bmfp_batch_s> b (new (std::nothrow) bmfp_batch_s);
+  if (!b)
+    return fail (BMFP_ERROR_OUT_OF_MEMORY, "host allocation failed");
+  b->n = n;
+  const int rc = b->engine.init (n, reinterpret_cast<const bmfp_matrix_s *const *> (mats), o, as_stream (stream));
+  if (rc != BMFP_SUCCESS)
+    return rc;
+  *out = b.release ();
+  return BMFP_SUCCESS;
+}
+
+int bmfp_batch_configure (bmfp_batch_t b, int cluster_size, int threads_per_cta)
+{
+  if (!b)
+    return fail (BMFP_ERROR_INVALID_VALUE, "null batch");
+  return b->engine.configure (cluster_size, threads_per_cta);
+}
+
+int bmfp_batch_autotune (bmfp_batch_t b, const void *const *d_b, void *const *d_x, int probe_iterations,
+                         int *cluster_size, int *threads_per_cta, void *stream)
+{
+  if (!b || (b->n > 0 && (!d_b || !d_x)) || probe_iterations < 1)
+    return fail (BMFP_ERROR_INVALID_VALUE, "invalid arguments");
+  const int rc = b->engine.autotune (d_b, d_x, as_stream (stream), probe_iterations);
+  if (cluster_size)
+    *cluster_size = b->engine.cluster ();
+  if (threads_per_cta)
+    *threads_per_cta = b->engine.threads ();
+  return rc;
+}
+
+int bmfp_batch_solve (bmfp_batch_t b, const void *const *d_b, void *const *d_x, bmfp_solve_info *infos,
+                      void *stream)
+{
+  if (!b || (b->n > 0 && (!d_b || !d_x || !infos)))
+    return fail (BMFP_ERROR_INVALID_VALUE, "invalid arguments");
+  if (b->n == 0)
+    return BMFP_SUCCESS;
+  const int rc = b->engine.solve (d_b, d_x, infos, as_stream (stream));
+  if (rc != BMFP_SUCCESS && rc != BMFP_ERROR_NOT_CONVERGED && rc != BMFP_ERROR_BREAKDOWN)
+    return rc;
+  if (rc != BMFP_SUCCESS)
+    fail (rc, "at least one batched system did not converge");
+  return rc;
+}
+
+int bmfp_batch_destroy (bmfp_batch_t b)
+{
+  delete b;
   return BMFP_SUCCESS;
 }
 

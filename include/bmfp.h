@@ -269,6 +269,89 @@ BMFP_API int bmfp_solver_solve (bmfp_solver_t s, const void *d_b, void *d_x, bmf
                                 void *stream);
 BMFP_API int bmfp_solver_destroy (bmfp_solver_t s);
 
+/* -------------------------------------------------------------- batched ---
+ * Many independent square systems of uneven size solved by ONE persistent
+ * kernel launch, captured with its work-queue reset in a CUDA graph. Teams
+ * of 1-8 CTAs (a thread-block cluster on as many SMs) take systems largest
+ * first and solve each one alone, with cluster barriers between phases and
+ * dot products reduced through distributed shared memory in a fixed order:
+ * a system's result is bitwise the same whatever else is in the batch, for a
+ * given configuration. Options as for bmfp_solver_create (FP64, FP32 or
+ * MIXED; no preconditioner). Matrices must be FP64 handles with bs <= 32 and
+ * must outlive the batch. No counterpart in the reference, which solves one
+ * CSR system per call (gpu/bicgstab.cu:387-526). */
+typedef struct bmfp_batch_s *bmfp_batch_t;
+
+BMFP_API int bmfp_batch_create (bmfp_batch_t *out, int n_systems, const bmfp_matrix_t *matrices,
+                                const bmfp_solver_options *opts, void *stream);
+/* Cluster size (1, 2, 4, 8) and threads per CTA (multiple of 64, <= 1024). */
+BMFP_API int bmfp_batch_configure (bmfp_batch_t b, int cluster_size, int threads_per_cta);
+/* The project's autotuner: times every (cluster, threads) candidate on this
+ * batch with each system capped at probe_iterations and keeps the fastest.
+ * Outputs may be NULL. Synchronises the stream. */
+BMFP_API int bmfp_batch_autotune (bmfp_batch_t b, const void *const *d_b, void *const *d_x,
+                                  int probe_iterations, int *cluster_size, int *threads_per_cta,
+                                  void *stream);
+/* Solve every system: d_b[i], d_x[i] are FP64 device vectors (host arrays of
+ * n_systems device pointers). infos[i] receives each system's result. Blocks
+ * until done; returns BMFP_SUCCESS when every system converged, else the
+ * first failing system's status. */
+BMFP_API int bmfp_batch_solve (bmfp_batch_t b, const void *const *d_b, void *const *d_x,
+                               bmfp_solve_info *infos, void *stream);
+BMFP_API int bmfp_batch_destroy (bmfp_batch_t b);
+
+/* -------------------------------------------------------------- serving ---
+ * Continuous batching of solve requests on one GPU (no counterpart in the
+ * reference). Requests (a resident FP64 matrix handle and a host right-hand
+ * side) are admitted in arrival order while their device memory fits the HBM
+ * budget and the in-flight limit, and what was admitted is launched at once
+ * as a micro-batch of the batched kernel on one of several streams, so new
+ * requests start while earlier ones are still on the GPU. Requests with more
+ * than wide_threshold_rows rows run on the whole-GPU engine. Matrices stay
+ * resident (the caller keeps the handles alive until the server is
+ * destroyed); each request's Krylov state lives on the device from admission
+ * to completion. A request's result does not depend on the other requests in
+ * flight. Thread-safe: submit, poll and wait may be called from any thread. */
+typedef struct bmfp_server_s *bmfp_server_t;
+
+typedef struct bmfp_server_options
+{
+  size_t hbm_budget_bytes;     /* device bytes for admitted requests (default 120 GiB) */
+  int max_in_flight;           /* requests on the device at once (default 4096) */
+  int max_batch;               /* requests per micro-batch launch (default 64) */
+  int streams;                 /* micro-batch streams (default 8) */
+  int cluster_size;            /* CTAs per system team (default 4) */
+  int threads_per_cta;         /* default 256 */
+  int64_t wide_threshold_rows; /* larger requests use the whole-GPU engine (default 200000) */
+  int wide_lanes;              /* whole-GPU solves run concurrently (default 4) */
+  bmfp_solver_options solver;  /* precision, tolerance, limits; no preconditioner */
+} bmfp_server_options;
+
+typedef struct bmfp_server_stats
+{
+  uint64_t submitted, completed, micro_batches, wide_solves;
+  size_t bytes_in_use, peak_bytes;
+  int in_flight, pending;
+} bmfp_server_stats;
+
+BMFP_API void bmfp_server_options_init (bmfp_server_options *opts);
+/* Start the dispatcher on the current device. */
+BMFP_API int bmfp_server_create (bmfp_server_t *out, const bmfp_server_options *opts);
+/* Queue a request; h_b is copied, h_x (n doubles) is written on completion
+ * and must stay valid until then. BMFP_ERROR_BUDGET if the request alone can
+ * never fit the budget. */
+BMFP_API int bmfp_server_submit (bmfp_server_t s, bmfp_matrix_t A, const double *h_b, double *h_x,
+                                 uint64_t *ticket);
+/* BMFP_PENDING while running; otherwise the request's final status, with
+ * info filled (info->seconds = submit-to-completion latency) and the ticket
+ * released. */
+BMFP_API int bmfp_server_poll (bmfp_server_t s, uint64_t ticket, bmfp_solve_info *info);
+/* As poll, but blocks until the request completes. */
+BMFP_API int bmfp_server_wait (bmfp_server_t s, uint64_t ticket, bmfp_solve_info *info);
+BMFP_API int bmfp_server_get_stats (bmfp_server_t s, bmfp_server_stats *stats);
+/* Finish every queued request, then stop and free the server. */
+BMFP_API int bmfp_server_destroy (bmfp_server_t s);
+
 /* BiCGStab that allocates nothing. No counterpart in the reference: it is
  * for callers that cannot call cudaMalloc (a device-memory pool or budget
  * that forbids more allocations, real-time loops that cannot take an

@@ -1,0 +1,120 @@
+"""Continuous-batching server: requests admitted under an HBM budget while
+others run, each result the same alone and in the mix."""
+import threading
+import time
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import block_matrix_format_performance_gb300 as bm
+
+pytestmark = pytest.mark.gpu
+
+GRIDS = [(20, 5), (40, 10), (64, 16), (30, 8), (80, 20), (24, 6), (52, 13), (100, 25)]
+
+
+@pytest.fixture(scope="module")
+def problems(lib, cuda):
+    out = []
+    for nx, ny in GRIDS:
+        rp, c, v, rhs = bm.gen_q4_elasticity(nx, ny)
+        out.append((bm.Matrix.from_bcsr(rp, c, v, 2), rp, c, v, rhs))
+    return out
+
+
+def loads(n, seed):
+    return np.random.default_rng(seed).uniform(-1, 1, n)
+
+
+def rel_residual(rp, c, v, b, x):
+    crp, cc, cv = bm.bcsr_to_csr(rp, c, v, 2)
+    K = sp.csr_matrix((cv, cc, crp))
+    return np.linalg.norm(b - K @ x) / np.linalg.norm(b)
+
+
+def test_mix_equals_alone_bitwise(problems):
+    mix = bm.Server("fp64", tol=1e-10, max_batch=3)
+    reqs = []
+    # submit from two threads with small gaps, so requests join while others run
+    def producer(idx):
+        for k in idx:
+            m, rp, c, v, _ = problems[k % len(problems)]
+            b = loads(m.rows, 100 + k)
+            x = np.full(m.rows, np.nan)
+            reqs.append((k, b, x, mix.submit(m, b, x)))
+            time.sleep(0.0005)
+    threads = [threading.Thread(target=producer, args=(range(i, 16, 2),)) for i in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    results = {k: (b, x, mix.wait(t)) for k, b, x, t in reqs}
+    stats = mix.stats()
+    assert stats["completed"] == 16 and stats["micro_batches"] >= 2 and stats["in_flight"] == 0
+    mix.close()
+    for k, (b, x, info) in sorted(results.items())[:8]:
+        m, rp, c, v, _ = problems[k % len(problems)]
+        assert info["status"] == bm.SUCCESS, info
+        assert rel_residual(rp, c, v, b, x) < 1e-10
+        alone = bm.Server("fp64", tol=1e-10)
+        x1 = np.full(m.rows, np.nan)
+        i1 = alone.wait(alone.submit(m, b, x1))
+        alone.close()
+        assert i1["iterations"] == info["iterations"]
+        assert np.array_equal(x.view(np.uint64), x1.view(np.uint64)), k
+
+
+def test_admission_respects_the_budget(problems):
+    m, rp, c, v, _ = problems[4]  # 80x20 -> 3200 rows
+    per_request = 256 * 2 * ((m.rows * 8 + 255) // 256) + ((m.rows * 64 + 255) // 256) * 256
+    srv = bm.Server("fp64", tol=1e-10, hbm_budget_bytes=int(2.5 * per_request))
+    xs = [np.zeros(m.rows) for _ in range(6)]
+    bs = [loads(m.rows, k) for k in range(6)]
+    tickets = [srv.submit(m, b, x) for b, x in zip(bs, xs)]
+    infos = [srv.wait(t) for t in tickets]
+    st = srv.stats()
+    srv.close()
+    assert all(i["status"] == bm.SUCCESS for i in infos)
+    assert st["peak_bytes"] <= int(2.5 * per_request)
+    for b, x in zip(bs, xs):
+        assert rel_residual(rp, c, v, b, x) < 1e-10
+
+
+def test_request_larger_than_budget_is_refused(problems):
+    m = problems[7][0]
+    srv = bm.Server("fp64", hbm_budget_bytes=1024)
+    with pytest.raises(bm.BmfpError) as e:
+        srv.submit(m, np.ones(m.rows), np.zeros(m.rows))
+    assert e.value.status == bm.ERROR_BUDGET
+    srv.close()
+
+
+def test_large_requests_take_the_whole_gpu_lane(problems):
+    srv = bm.Server("fp64", tol=1e-10, wide_threshold_rows=3000)
+    todo = []
+    for k in (7, 0, 4, 1):  # 100x25 and 80x20 go wide, the others batch
+        m, rp, c, v, _ = problems[k]
+        b = loads(m.rows, k)
+        x = np.zeros(m.rows)
+        todo.append((rp, c, v, b, x, srv.submit(m, b, x)))
+    for rp, c, v, b, x, t in todo:
+        info = srv.wait(t)
+        assert info["status"] == bm.SUCCESS and rel_residual(rp, c, v, b, x) < 1e-10
+    st = srv.stats()
+    srv.close()
+    assert st["wide_solves"] == 2 and st["micro_batches"] >= 1
+
+
+def test_mixed_precision_server(problems):
+    srv = bm.Server("mixed", tol=1e-10)
+    todo = []
+    for k in (0, 1, 5):
+        m, rp, c, v, _ = problems[k]
+        b = loads(m.rows, k)
+        x = np.zeros(m.rows)
+        todo.append((rp, c, v, b, x, srv.submit(m, b, x)))
+    for rp, c, v, b, x, t in todo:
+        info = srv.wait(t)
+        assert info["status"] == bm.SUCCESS and rel_residual(rp, c, v, b, x) < 1e-10
+    srv.close()
