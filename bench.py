@@ -75,8 +75,6 @@ def parse_args():
     ap.add_argument("--systems", type=int, default=256, help="batch: number of systems")
     ap.add_argument("--requests", type=int, default=1000, help="serve: number of requests")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (req/s)")
-    ap.add_argument("--baseline-requests", type=int, default=200,
-                    help="serve: requests of the same stream timed on the plain FP64 per-request solver")
     ap.add_argument("--grid", default="200x50", help="solve: nodes nx x ny of the Q4 grid")
     ap.add_argument("--precision", default="fp64", choices=("fp64", "fp32", "mixed"))
     ap.add_argument("--tol", type=float, default=1e-10)
@@ -606,24 +604,26 @@ def run_serve(args):
     srv.close()
     lat = np.array([i["seconds"] for i in infos])
     conv = sum(i["status"] == 0 for i in infos)
-    # baseline: plain FP64 per-request solver, FIFO on one GPU, same stream head
-    nb = min(args.baseline_requests, len(grids))
-    solvers = {}
-    service = []
-    for k in range(nb):
-        g = grids[k]
-        if g not in solvers:
-            solvers[g] = bm.Solver(mats[g], "fp64", tol=args.tol, max_iters=args.max_iters)
+    # Baseline: the plain FP64 per-request solver serving the same stream FIFO
+    # on one GPU. Each distinct grid's solve is timed once on the device and
+    # the queue is replayed with those service times.
+    solvers, service_by_grid = {}, {}
+    for k, g in enumerate(grids):
+        if g in service_by_grid:
+            continue
+        s = bm.Solver(mats[g], "fp64", tol=args.tol, max_iters=args.max_iters)
         d_b = torch.from_numpy(rhs[k]).cuda()
         d_x = torch.empty_like(d_b)
         t0 = time.perf_counter()
-        solvers[g].solve(d_b, d_x)
-        service.append(time.perf_counter() - t0)
+        s.solve(d_b, d_x)
+        service_by_grid[g] = time.perf_counter() - t0
+        s.close()
     done, base_lat = 0.0, []
-    for k in range(nb):
-        done = max(done, arrivals[k]) + service[k]
+    for k, g in enumerate(grids):
+        done = max(done, arrivals[k]) + service_by_grid[g]
         base_lat.append(done - arrivals[k])
-    base_tput = nb / max(done, 1e-9)
+    base_tput = len(grids) / max(done, 1e-9)
+    nb = len(grids)
     print(json.dumps({
         "workload": "serve", "requests": len(grids), "rate_req_s": args.rate, "precision": args.precision,
         "tol": args.tol, "large_requests": int(sum(g == (1000, 250) for g in grids)),
@@ -632,7 +632,8 @@ def run_serve(args):
         "converged": conv, "worst_true_rel": max(i["true_rel_residual"] for i in infos),
         "micro_batches": stats["micro_batches"], "wide_solves": stats["wide_solves"],
         "peak_device_bytes": stats["peak_bytes"],
-        "per_request_fp64": {"requests": nb, "solves_per_s": round(base_tput, 2),
+        "per_request_fp64": {"requests": nb, "distinct_grids_timed": len(service_by_grid),
+                             "solves_per_s": round(base_tput, 2),
                              "latency_p50_s": round(float(np.percentile(base_lat, 50)), 4),
                              "latency_p99_s": round(float(np.percentile(base_lat, 99)), 4)}}), flush=True)
 

@@ -167,7 +167,7 @@ int bmfp_bcsr_spmv_native_ex (int dtype, int n_block_rows, int bs, int64_t nnzb,
 {
   if (!dtype_ok (dtype))
     return fail (BMFP_ERROR_INVALID_VALUE, "invalid dtype %d", dtype);
-  if (n_block_rows < 0 || nnzb < 0 || bs < 1 || lanes < 0 || lanes > 32)
+  if (n_block_rows < 0 || nnzb < 0 || bs < 1 || lanes < 0 || (lanes > 32 && lanes != BMFP_LANES_ROW_OWNER))
     return fail (BMFP_ERROR_INVALID_VALUE, "invalid arguments");
   if (n_block_rows == 0)
     return BMFP_SUCCESS;
@@ -404,9 +404,9 @@ int bmfp_matrix_autotune (bmfp_matrix_t m, const void *d_x, void *d_y, void *str
 {
   if (!m || !d_x || !d_y)
     return fail (BMFP_ERROR_INVALID_VALUE, "null argument");
-  int cand[8];
+  int cand[10];
   const int bs_eff = m->bs ? m->bs : 1;
-  int nc = native_lane_candidates (m->dtype, bs_eff, cand, 8);
+  int nc = native_lane_candidates (m->dtype, bs_eff, cand, 10);
   if (nc == 0)
     {
       if (chosen_lanes)

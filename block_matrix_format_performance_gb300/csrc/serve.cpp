@@ -378,9 +378,12 @@ void bmfp_server_options_init (bmfp_server_options *o)
   o->hbm_budget_bytes = (size_t) 120 << 30;
   o->max_in_flight = 4096;
   o->max_batch = 64;
-  o->streams = 8;
+  o->streams = 48;
   o->cluster_size = 4;
   o->threads_per_cta = 256;
+  // Above 200 000 rows a 4-CTA team takes tens of milliseconds per iteration
+  // and can wander to the iteration cap (measured on 500 000-row elasticity
+  // requests); the whole-GPU engine finishes them in about 0.35 s.
   o->wide_threshold_rows = 200000;
   o->wide_lanes = 4;
   bmfp_solver_options_init (&o->solver);

@@ -172,6 +172,53 @@ __device__ __forceinline__ void flat_row (int row, const int *__restrict__ row_p
     }
 }
 
+// One block row by BS lanes, lane r owning scalar row r: it streams row r of
+// every block (BS/V 16-byte vectors, read through L1 so the two halves of a
+// sector meet there) against the block's x segment (the same addresses in
+// every lane of the group). Each lane finishes its own row: no cross-lane
+// reduction, so every FP64 instruction is a useful FMA — what GB300's narrow
+// FP64 pipe needs. Requires bs a multiple of V and 16-byte aligned values/x.
+template <typename T, int BS, class Epi>
+__device__ __forceinline__ void rowown_row (int row, const int *__restrict__ row_ptr,
+                                            const int *__restrict__ cols, const T *__restrict__ vals,
+                                            const T *__restrict__ x, T *__restrict__ y, Epi &epi)
+{
+  using V16 = dev::Vec16<T>;
+  constexpr int V = V16::N;
+  constexpr int NV = BS / V; // vectors per block line
+  static_assert (BS % V == 0, "block line must be whole 16-byte vectors");
+  const int r = threadIdx.x & (BS - 1);
+  const int beg = __ldg (row_ptr + row);
+  const int end = __ldg (row_ptr + row + 1);
+  T acc0 = 0, acc1 = 0;
+  for (int b = beg; b < end; b++)
+    {
+      const T *line = vals + (size_t) b * BS * BS + (size_t) r * BS;
+      const T *xs = x + (size_t) __ldg (cols + b) * BS;
+      V16 a[NV];
+#pragma unroll
+      for (int k = 0; k < NV; k++)
+        a[k] = dev::ld_cached16 (line + k * V);
+#pragma unroll
+      for (int k = 0; k < NV; k++)
+        {
+          const V16 xv = dev::ld_cached16 (xs + k * V);
+#pragma unroll
+          for (int v = 0; v < V; v++)
+            {
+              if ((k * V + v) & 1)
+                acc1 = fma (a[k].v[v], xv.v[v], acc1);
+              else
+                acc0 = fma (a[k].v[v], xv.v[v], acc0);
+            }
+        }
+    }
+  const T acc = acc0 + acc1;
+  const int64_t i = (int64_t) row * BS + r;
+  y[i] = acc;
+  epi (i, acc);
+}
+
 // One block row by a whole warp, lane (q, r) = (lane / bs, lane % bs), any
 // bs <= 32; scalar loads (no alignment requirement).
 template <typename T, int BSC, class Epi>

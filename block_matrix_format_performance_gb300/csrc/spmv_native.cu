@@ -51,6 +51,19 @@ __global__ void __launch_bounds__ (kThreads)
     core::flat_row<T, BS, G, U> ((int) row, row_ptr, cols, vals, x, y, epi);
 }
 
+// Row-owner mapping: BS lanes per block row, one per scalar row.
+template <typename T, int BS>
+__global__ void __launch_bounds__ (kThreads)
+  bcsr_rowown_kernel (int n_block_rows, const int *__restrict__ row_ptr, const int *__restrict__ cols,
+                      const T *__restrict__ vals, const T *__restrict__ x, T *__restrict__ y)
+{
+  const int64_t group = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) / BS;
+  const int64_t n_groups = (int64_t) gridDim.x * blockDim.x / BS;
+  core::NoEpilogue epi;
+  for (int64_t row = group; row < n_block_rows; row += n_groups)
+    core::rowown_row<T, BS> ((int) row, row_ptr, cols, vals, x, y, epi);
+}
+
 template <typename T, int BSC>
 __global__ void __launch_bounds__ (kThreads)
   bcsr_tpr_kernel (int n_block_rows, int bs_rt, const int *__restrict__ row_ptr,
@@ -183,6 +196,23 @@ int native_bcsr_typed (int nbr, int bs, int64_t nnzb, const int *rp, const int *
   const int dtype = sizeof (T) == 8 ? BMFP_R64F : BMFP_R32F;
   if (bs == 1)
     return launch_csr<T> (nbr, lanes ? lanes : csr_default_lanes (avg), rp, c, v, x, y, s);
+  if (lanes == BMFP_LANES_ROW_OWNER)
+    {
+      const bool ok = (reinterpret_cast<uintptr_t> (v) | reinterpret_cast<uintptr_t> (x)) % 16 == 0;
+      if (!ok || !(bs == 4 || bs == 8 || bs == 16 || bs == 32))
+        return fail (BMFP_ERROR_INVALID_VALUE, "row-owner mapping needs bs in {4,8,16,32} and aligned arrays");
+      const int64_t threads = (int64_t) nbr * bs;
+      const unsigned grid = (unsigned) ((threads + kThreads - 1) / kThreads);
+      switch (bs)
+        {
+        case 4: bcsr_rowown_kernel<T, 4><<<grid, kThreads, 0, s>>> (nbr, rp, c, v, x, y); break;
+        case 8: bcsr_rowown_kernel<T, 8><<<grid, kThreads, 0, s>>> (nbr, rp, c, v, x, y); break;
+        case 16: bcsr_rowown_kernel<T, 16><<<grid, kThreads, 0, s>>> (nbr, rp, c, v, x, y); break;
+        default: bcsr_rowown_kernel<T, 32><<<grid, kThreads, 0, s>>> (nbr, rp, c, v, x, y); break;
+        }
+      BMFP_LAUNCH_CHECK ();
+      return BMFP_SUCCESS;
+    }
   // The flat kernel issues 16-byte vector loads of values and x: it needs
   // both base pointers 16-byte aligned (cudaMalloc gives 256). Misaligned
   // views fall through to the scalar-load kernel below.
@@ -266,6 +296,8 @@ int native_lane_candidates (int dtype, int bs, int *out, int max_out)
   for (int g = 2; g <= 32 && n < max_out; g <<= 1)
     if (flat_lanes_ok (dtype, bs, g))
       out[n++] = g;
+  if (bs >= 4 && n < max_out)
+    out[n++] = BMFP_LANES_ROW_OWNER;
   return n;
 }
 

@@ -146,8 +146,11 @@ BMFP_API int bmfp_bcsr_spmv (int dtype, int variant, int n_block_rows, int n_blo
 
 /* Lanes per block row the native kernel would use for this shape (0 = the
  * built-in heuristic); lets callers and the autotuner pin the choice.
- * Valid group sizes: 0, 2, 4, 8, 16, 32 (clamped to what the block size
- * allows). Affects only BMFP_SPMV_BCSR_NATIVE. */
+ * Valid values: 0, 2, 4, 8, 16, 32 (a group of that many lanes walks the
+ * block row's values in 16-byte vectors; needs lanes * 16 bytes >= one block
+ * line), or BMFP_LANES_ROW_OWNER (bs in {4,8,16,32}: one lane per scalar
+ * row, no cross-lane reduction). Affects only BMFP_SPMV_BCSR_NATIVE. */
+#define BMFP_LANES_ROW_OWNER 64
 BMFP_API int bmfp_bcsr_spmv_native_ex (int dtype, int n_block_rows, int bs, int64_t nnzb,
                                        const int *d_row_ptr, const int *d_cols,
                                        const void *d_values, const void *d_x, void *d_y,
@@ -307,7 +310,7 @@ BMFP_API int bmfp_batch_destroy (bmfp_batch_t b);
  * budget and the in-flight limit, and what was admitted is launched at once
  * as a micro-batch of the batched kernel on one of several streams, so new
  * requests start while earlier ones are still on the GPU. Requests with more
- * than wide_threshold_rows rows run on the whole-GPU engine. Matrices stay
+ * than wide_threshold_rows rows run on whole-GPU engine lanes. Matrices stay
  * resident (the caller keeps the handles alive until the server is
  * destroyed); each request's Krylov state lives on the device from admission
  * to completion. A request's result does not depend on the other requests in
@@ -319,7 +322,7 @@ typedef struct bmfp_server_options
   size_t hbm_budget_bytes;     /* device bytes for admitted requests (default 120 GiB) */
   int max_in_flight;           /* requests on the device at once (default 4096) */
   int max_batch;               /* requests per micro-batch launch (default 64) */
-  int streams;                 /* micro-batch streams (default 8) */
+  int streams;                 /* micro-batch streams (default 48) */
   int cluster_size;            /* CTAs per system team (default 4) */
   int threads_per_cta;         /* default 256 */
   int64_t wide_threshold_rows; /* larger requests use the whole-GPU engine (default 200000) */

@@ -129,10 +129,12 @@ def test_native_every_lane_count(lib, orc, cuda, bs, dtype):
     crp, cc, cv = orc.bcsr_to_csr(rp, c, v, bs)
     tol = spmv_tolerance(orc, crp, cc, cv, x, dtype)
     vec = 2 if dtype == np.float64 else 4
-    for g in (2, 4, 8, 16, 32):
+    for g in (2, 4, 8, 16, 32, 64):  # 64 = BMFP_LANES_ROW_OWNER (one lane per scalar row)
+        if g == 64 and bs < 4:
+            continue
         d_y = torch.full((nbr * bs + GUARD,), float("nan"), dtype=torch.float64 if dtype == np.float64 else torch.float32,
                          device="cuda")
-        if g * vec < bs:
+        if g != 64 and g * vec < bs:
             with pytest.raises(bm.BmfpError):
                 bm.bcsr_spmv_native(dev(rp), dev(c), dev(v), dev(x), d_y, bs, lanes=g)
             continue
@@ -192,7 +194,7 @@ def test_matrix_handle_upload_autotune_convert(lib, orc, cuda, bs):
     d_x = dev(x)
     d_y = torch.empty(2000 * bs, dtype=torch.float64, device="cuda")
     lanes = m.autotune(d_x, d_y)
-    assert lanes in (2, 4, 8, 16, 32)
+    assert lanes in (2, 4, 8, 16, 32, 64)
     m.spmv(d_x, d_y)
     y_ref = orc.bcsr_spmv(rp, c, v, bs, x)
     crp, cc, cv = orc.bcsr_to_csr(rp, c, v, bs)
