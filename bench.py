@@ -65,6 +65,8 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-csr-compare", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="use the built-in lane choices (the autotuner's GB300 picks) instead of timing candidates")
     ap.add_argument("--sizes", default=",".join(map(str, BLOCK_SIZES)))
     ap.add_argument("--dtypes", default=",".join(DTYPES))
     ap.add_argument("--n-block-rows", type=int, default=NBR,
@@ -224,7 +226,7 @@ def run_ours(args):
         cs["dx"] = torch.from_numpy(cs["x"]).cuda()
         cs["dy"] = torch.empty_like(cs["dx"])
         # the library's autotuner times every valid lane count on this matrix
-        cs["lanes"] = cs["m"].autotune(cs["dx"], cs["dy"])
+        cs["lanes"] = 0 if args.no_autotune else cs["m"].autotune(cs["dx"], cs["dy"])
     flush_w = torch.empty(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB
     flush_r = torch.ones(128 << 20, dtype=torch.float32, device="cuda")  # 512 MB
 

@@ -195,7 +195,14 @@ int native_bcsr_typed (int nbr, int bs, int64_t nnzb, const int *rp, const int *
   const double avg = nbr > 0 ? (double) nnzb / nbr : 0.0;
   const int dtype = sizeof (T) == 8 ? BMFP_R64F : BMFP_R32F;
   if (bs == 1)
-    return launch_csr<T> (nbr, lanes ? lanes : csr_default_lanes (avg), rp, c, v, x, y, s);
+    return launch_csr<T> (nbr, lanes ? lanes : native_default_lanes (dtype, 1, avg), rp, c, v, x, y, s);
+  if (lanes == 0 && flat_bs (bs))
+    {
+      lanes = native_default_lanes (dtype, bs, avg);
+      const bool ok = (reinterpret_cast<uintptr_t> (v) | reinterpret_cast<uintptr_t> (x)) % 16 == 0;
+      if (lanes == BMFP_LANES_ROW_OWNER && (!ok || bs < 4))
+        lanes = 0; // misaligned views: the scalar-load kernel below
+    }
   if (lanes == BMFP_LANES_ROW_OWNER)
     {
       const bool ok = (reinterpret_cast<uintptr_t> (v) | reinterpret_cast<uintptr_t> (x)) % 16 == 0;
@@ -253,33 +260,36 @@ int native_bcsr_typed (int nbr, int bs, int64_t nnzb, const int *rp, const int *
 int native_default_lanes (int dtype, int bs, double avg_blocks_per_row)
 {
   if (bs == 1)
-    return csr_default_lanes (avg_blocks_per_row);
+    {
+      // A few lanes per CSR row: the autotuner picked 1-2 on GB300 for eight
+      // entries per row.
+      int g = 1;
+      while (g < 32 && 4 * g < avg_blocks_per_row)
+        g <<= 1;
+      return g;
+    }
   if (!flat_bs (bs))
     return 32;
+  // The choices bmfp_matrix_autotune made on GB300 for the block-size sweep
+  // (100 000 block rows, 8 blocks per row). FP64 is bound by GB300's narrow
+  // FP64 pipe, where a warp instruction costs the same however many lanes are
+  // active, so from bs 8 on one lane owns one scalar row (no shuffle adds).
   if (dtype == BMFP_R64F)
     {
-      // FP64 products are bound by GB300's narrow FP64 pipe, where a warp
-      // instruction costs the same whether 2 or 32 lanes are active: give
-      // each lane whole block lines (no predicated-off lanes, few shuffle
-      // adds): bs 2 -> 2 lanes, 4 -> 4, 8 -> 4, 16 -> 8, 32 -> 16.
       switch (bs)
         {
-        case 2: return 2;
+        case 2: return 4;
         case 4: return 4;
-        case 8: return 4;
-        case 16: return 8;
-        default: return 16;
+        default: return BMFP_LANES_ROW_OWNER;
         }
     }
-  // Aim for about two 16-byte vectors per lane per block row, within the
-  // lane counts this block size allows.
-  const double vectors = avg_blocks_per_row * bs * bs / vec_elems (dtype);
-  int g = 2;
-  while (g < 32 && 2.0 * g < vectors)
-    g <<= 1;
-  while (!flat_lanes_ok (dtype, bs, g) && g < 32)
-    g <<= 1;
-  return g;
+  switch (bs)
+    {
+    case 2: return 2;
+    case 4: return BMFP_LANES_ROW_OWNER;
+    case 8: return 8;
+    default: return 32;
+    }
 }
 
 int native_lane_candidates (int dtype, int bs, int *out, int max_out)

@@ -78,14 +78,14 @@ def test_invalid_arguments_fail_without_touching_a_device(lib):
 
 
 def test_native_lane_heuristic(lib):
-    assert bm.native_default_lanes(np.float64, 2, 8.0) == 2
-    assert bm.native_default_lanes(np.float64, 32, 8.0) == 16
-    assert bm.native_default_lanes(np.float32, 2, 8.0) == 4
+    assert bm.native_default_lanes(np.float64, 2, 8.0) == 4
+    assert bm.native_default_lanes(np.float64, 32, 8.0) == 64  # one lane per scalar row
+    assert bm.native_default_lanes(np.float32, 2, 8.0) == 2
     for bs in (2, 4, 8, 16, 32):
         for dt in (np.float32, np.float64):
             g = bm.native_default_lanes(dt, bs, 8.0)
             v = 2 if dt == np.float64 else 4
-            assert g in (2, 4, 8, 16, 32) and g * v >= bs
+            assert g == 64 or (g in (2, 4, 8, 16, 32) and g * v >= bs)
 
 
 def test_oracle_is_not_linked_into_the_product(lib):
