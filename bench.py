@@ -65,6 +65,7 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-csr-compare", action="store_true")
+    ap.add_argument("--no-solver", action="store_true", help="skip the batched-solve part of the line")
     ap.add_argument("--no-autotune", action="store_true",
                     help="use the built-in lane choices (the autotuner's GB300 picks) instead of timing candidates")
     ap.add_argument("--sizes", default=",".join(map(str, BLOCK_SIZES)))
@@ -92,6 +93,23 @@ def np_dt(tag):
 def case_bytes(bs, tag, nnzb, nbr=NBR):
     S = 8 if tag == "f64" else 4
     return nnzb * bs * bs * S + nnzb * 4 + (nbr + 1) * 4 + 2 * nbr * bs * S
+
+
+def max_over_ranks(value, dist, device):
+    """Largest per-rank value (the slowest replica's time); the value itself on
+    a single process. Replicas exchange only this scalar — no data-path
+    collective."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(total_bytes_per_rank, world, t_max_s):
+    """Whole-job GB/s: every rank's bytes over the slowest rank's time."""
+    return world * total_bytes_per_rank / t_max_s / 1e9
 
 
 def dist_env():
@@ -264,12 +282,8 @@ def run_ours(args):
 
     step_ms = sum(per_case_ms) / args.steps
     total_bytes = sum(cs["bytes"] for cs in cases)
-    t_max = step_ms
-    if dist:
-        t = torch.tensor([step_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = world * total_bytes / (t_max * 1e-3) / 1e9
+    t_max = max_over_ranks(step_ms, dist, "cuda")
+    value = replica_value(total_bytes, world, t_max * 1e-3)
 
     per_case = {}
     for i, cs in enumerate(cases):
@@ -340,15 +354,21 @@ def run_ours(args):
         for _ in range(args.e2e_steps):
             e2e_step()
         e2e_s = (time.perf_counter() - e0) / args.e2e_steps
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * total_bytes / e2e_s / 1e9
+    e2e_s = max_over_ranks(e2e_s, dist, "cuda")
+    e2e_value = replica_value(total_bytes, world, e2e_s)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(cases, nbr=nbr)
+
+    # Solver side of the metric: the uneven batch of elasticity systems at
+    # 1e-10, batched FP64 and mixed against the plain FP64 per-request solver.
+    solves = None
+    if not args.no_solver:
+        for cs in cases:
+            cs.pop("m", None)
+        torch.cuda.empty_cache()
+        solves = measure_batch(["fp64", "mixed"], 1e-10, 100000, 2)
 
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world,
@@ -373,6 +393,9 @@ def run_ours(args):
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if solves is not None:
+        line["solves"] = {"workload": "256 uneven Q4 plane-stress systems, nx log-uniform in [20,400], ny = nx/4, "
+                                      "bs 2, 1e-10 true relative residual", **solves}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -496,16 +519,14 @@ def batch_grids(n_systems, seed=0):
     return [(int(nx), max(2, int(round(nx / 4)))) for nx in nxs]
 
 
-def run_batch(args):
-    """Uneven batch: every system solved by one persistent, graph-captured
-    launch (precision --precision), against the plain FP64 per-request solver
-    run system after system."""
+def measure_batch(precisions, tol, max_iters, repeats, n_systems=256, per_request=True):
+    """The uneven batch (nx log-uniform in [20, 400], ny = nx / 4, seeded): each
+    precision solved by one persistent, graph-captured launch, and the plain
+    FP64 per-request solver run system after system on the same GPU."""
     import torch
 
     import block_matrix_format_performance_gb300 as bm
-    from block_matrix_format_performance_gb300 import build as B
-    B.build()
-    grids = batch_grids(args.systems)
+    grids = batch_grids(n_systems)
     mats, rhs = [], []
     for nx, ny in grids:
         rp, c, v, b = bm.gen_q4_elasticity(nx, ny)
@@ -513,39 +534,51 @@ def run_batch(args):
         rhs.append(b)
     d_b = [torch.from_numpy(b).cuda() for b in rhs]
     d_x = [torch.empty_like(b) for b in d_b]
-    batch = bm.Batch(mats, args.precision, tol=args.tol, max_iters=args.max_iters)
-    t0 = time.perf_counter()
-    cluster, threads = batch.autotune(d_b, d_x, probe_iterations=16)
-    tune_s = time.perf_counter() - t0
-    batch.solve(d_b, d_x)
-    times, infos = [], None
-    for _ in range(max(1, args.repeats)):
+    out = {"systems": len(grids), "dofs_total": int(sum(2 * a * b for a, b in grids)), "tol": tol}
+    for prec in precisions:
+        batch = bm.Batch(mats, prec, tol=tol, max_iters=max_iters)
         t0 = time.perf_counter()
-        infos = batch.solve(d_b, d_x)
-        times.append(time.perf_counter() - t0)
-    batch_s = min(times)
-    per_request_s = None
-    seq_infos = []
-    if args.repeats > 0:
+        cluster, threads = batch.autotune(d_b, d_x, probe_iterations=16)
+        tune_s = time.perf_counter() - t0
+        batch.solve(d_b, d_x)
+        times, infos = [], None
+        for _ in range(max(1, repeats)):
+            t0 = time.perf_counter()
+            infos = batch.solve(d_b, d_x)
+            times.append(time.perf_counter() - t0)
+        batch.close()
+        batch_s = min(times)
+        out[prec] = {
+            "cluster": cluster, "threads_per_cta": threads, "autotune_s": round(tune_s, 3),
+            "batch_s": round(batch_s, 4), "solves_per_s": round(len(grids) / batch_s, 2),
+            "converged": sum(i["status"] == 0 for i in infos),
+            "worst_true_rel": max(i["true_rel_residual"] for i in infos),
+            "iterations": sum(i["iterations"] for i in infos),
+            "iterations_fp32": sum(i["iterations_fp32"] for i in infos),
+            "fp64_fallbacks": sum(i["used_fp64_fallback"] for i in infos),
+            "not_converged": [{"grid": grids[k], "true_rel": i["true_rel_residual"]} for k, i in enumerate(infos)
+                              if i["status"] != 0][:12]}
+    if per_request:
+        seq = []
         t0 = time.perf_counter()
         for m, b, x in zip(mats, d_b, d_x):
-            s = bm.Solver(m, "fp64", tol=args.tol, max_iters=args.max_iters)
-            seq_infos.append(s.solve(b, x))
+            s = bm.Solver(m, "fp64", tol=tol, max_iters=max_iters)
+            seq.append(s.solve(b, x))
             s.close()
-        per_request_s = time.perf_counter() - t0
-    conv = sum(i["status"] == 0 for i in infos)
-    print(json.dumps({
-        "workload": "batch", "systems": len(grids), "dofs_total": int(sum(2 * a * b for a, b in grids)),
-        "precision": args.precision, "tol": args.tol, "cluster": cluster, "threads_per_cta": threads,
-        "autotune_s": round(tune_s, 3), "batch_s": round(batch_s, 4), "solves_per_s": round(len(grids) / batch_s, 2),
-        "converged": conv, "worst_true_rel": max(i["true_rel_residual"] for i in infos),
-        "iterations": sum(i["iterations"] for i in infos), "iterations_fp32": sum(i["iterations_fp32"] for i in infos),
-        "fp64_fallbacks": sum(i["used_fp64_fallback"] for i in infos),
-        "per_request_fp64_s": round(per_request_s, 4) if per_request_s else None,
-        "per_request_fp64_solves_per_s": round(len(grids) / per_request_s, 2) if per_request_s else None,
-        "per_request_fp64_converged": sum(i["status"] == 0 for i in seq_infos),
-        "not_converged": [{"grid": grids[k], "true_rel": i["true_rel_residual"]} for k, i in enumerate(infos)
-                          if i["status"] != 0][:20]}), flush=True)
+        dt = time.perf_counter() - t0
+        out["per_request_fp64"] = {"seconds": round(dt, 4), "solves_per_s": round(len(grids) / dt, 2),
+                                   "converged": sum(i["status"] == 0 for i in seq)}
+    for m in mats:
+        m.close()
+    return out
+
+
+def run_batch(args):
+    from block_matrix_format_performance_gb300 import build as B
+    B.build()
+    res = measure_batch([args.precision], args.tol, args.max_iters, args.repeats, args.systems,
+                        per_request=args.repeats > 0)
+    print(json.dumps({"workload": "batch", "precision": args.precision, **res}), flush=True)
 
 
 def serve_stream(n_requests, rate, seed=1):
