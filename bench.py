@@ -72,9 +72,14 @@ def parse_args():
     ap.add_argument("--dtypes", default=",".join(DTYPES))
     ap.add_argument("--n-block-rows", type=int, default=NBR,
                     help="block rows per matrix (smaller only for profiling captures)")
-    ap.add_argument("--workload", choices=("spmv", "solve", "batch", "serve"), default="spmv",
+    ap.add_argument("--workload", choices=("spmv", "solve", "batch", "serve", "ndiag"), default="spmv",
                     help="spmv: the block-size sweep line (default); solve: one Q4 elasticity solve; "
-                         "batch: 256 uneven Q4 systems in one persistent launch")
+                         "batch: 256 uneven Q4 systems in one persistent launch; serve: Poisson request "
+                         "stream through the server; ndiag: every variant on gen_n_diag_bcsr matrices, "
+                         "written in the reference's result.json layout")
+    ap.add_argument("--results-json", default=None, help="ndiag: write {bs: {format: seconds}} here")
+    ap.add_argument("--ndiag-rows", type=int, default=50_000, help="ndiag: block rows")
+    ap.add_argument("--ndiag-dtype", default="f32", choices=("f32", "f64"))
     ap.add_argument("--systems", type=int, default=256, help="batch: number of systems")
     ap.add_argument("--requests", type=int, default=1000, help="serve: number of requests")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (req/s)")
@@ -323,7 +328,10 @@ def run_ours(args):
                 "native_speedup": round(ms / (per_case_ms[cases.index(cs)] / args.steps), 2)}
             del d_rp, d_c, d_v
 
-    # End to end through the C ABI with host buffers.
+    # End to end through the C ABI with host buffers: bmfp_bcsr_spmv_host
+    # takes the pinned host arrays, uploads them in chunks overlapped with the
+    # product and returns y in host memory, so every step moves the whole
+    # matrix and x across the host link and y back.
     pinned = []
     for cs in cases:
         pinned.append(tuple(torch.from_numpy(a).pin_memory() for a in (cs["rp"], cs["c"], cs["v"], cs["x"])))
@@ -336,13 +344,7 @@ def run_ours(args):
 
     def e2e_step():
         for cs, p, hy in zip(cases, pinned, h_y):
-            m = bm.Matrix.from_bcsr(p[0].numpy(), p[1].numpy(), p[2].numpy(), cs["bs"])
-            dx = p[3].to("cuda", non_blocking=True)
-            dy = torch.empty_like(dx)
-            m.spmv(dx, dy)
-            hy.copy_(dy, non_blocking=True)
-            torch.cuda.synchronize()
-            m.close()
+            bm.bcsr_spmv_host(p[0].numpy(), p[1].numpy(), p[2].numpy(), p[3].numpy(), cs["bs"], y=hy.numpy())
 
     e2e_s = float("nan")
     if args.e2e_steps > 0:
@@ -673,6 +675,86 @@ def run_serve(args):
                              "latency_p99_s": round(float(np.percentile(base_lat, 99)), 4)}}), flush=True)
 
 
+def run_ndiag(args, sizes=(2, 4, 8, 16, 32), blocks_per_row=6, runs=10):
+    """The reference's default run (main.cpp:383-398 -> measure_diag_matrices,
+    main.cpp:318-344): gen_n_diag_bcsr matrices (FP32 by default, 50 000 block
+    rows, 6 blocks per row) for bs 2..32, every format timed `runs` times and
+    averaged (perform_measurements, main.cpp:131-148), kernels only between
+    CUDA events as gpu_matrix_multiplier.cu times them. The output map
+    {bs: {format: mean seconds}} is the layout of the reference's
+    results/result.json, which its plot/plot.py reads; "CPU CSR" is the
+    single-thread CPU loop (main.cpp:21-63), timed through the oracle's
+    restatement as the CPU baseline, and each GPU result is checked against it
+    with compare_results' rule (sum (a-b)^2 / sum b^2 <= 1e-9,
+    measurement_class.h:58-87)."""
+    import torch
+
+    import block_matrix_format_performance_gb300 as bm
+    from block_matrix_format_performance_gb300 import build as B
+    from oracle import oracle as orc
+    B.build()
+    orc.build()
+    dt = np_dt(args.ndiag_dtype)
+    n_rows = args.ndiag_rows
+    results, checks = {}, {}
+    stream = torch.cuda.current_stream()
+    for bs in sizes:
+        rp, c, v = bm.gen_n_diag_bcsr(n_rows, blocks_per_row, bs, dt)
+        crp, cc, cv = bm.bcsr_to_csr(rp, c, v, bs)
+        vt = bm.transpose_blocks(rp, v, bs)
+        x = np.ones(n_rows * bs, dtype=dt)  # main.cpp:27 sets x := 1
+        res = {}
+        y_ref = orc.csr_spmv(crp, cc, cv, x)
+        t0 = time.perf_counter()
+        for _ in range(runs):
+            orc.csr_spmv(crp, cc, cv, x)
+        res["CPU CSR"] = (time.perf_counter() - t0) / runs
+        d = {k: torch.from_numpy(a).cuda() for k, a in
+             (("rp", rp), ("c", c), ("v", v), ("vt", vt), ("crp", crp), ("cc", cc), ("cv", cv), ("x", x))}
+        dy = torch.empty(n_rows * bs, dtype=d["x"].dtype, device="cuda")
+        worst = 0.0
+        for var in range(bm.VARIANT_COUNT):
+            name = bm.variant_name(var)
+
+            def launch():
+                if bm.variant_is_csr(var):
+                    bm.csr_spmv(var, d["crp"], d["cc"], d["cv"], d["x"], dy)
+                else:
+                    vals = d["vt"] if bm.variant_layout(var) == 1 else d["v"]
+                    bm.bcsr_spmv(var, d["rp"], d["c"], vals, d["x"], dy, bs)
+            try:
+                launch()
+            except bm.BmfpError as e:
+                if e.status == bm.ERROR_NOT_SUPPORTED:
+                    continue  # e.g. the power-of-two variant at other bs, as gpu_matrix_multiplier.cu:1226
+                raise
+            torch.cuda.synchronize()
+            y = dy.cpu().numpy()
+            err = float(np.sum((y.astype(np.float64) - y_ref) ** 2) / np.sum(y_ref.astype(np.float64) ** 2))
+            worst = max(worst, err)
+            if err > 1e-9:
+                raise SystemExit(f"{name} bs {bs}: compare_results error {err:.3e}")
+            tot = 0.0
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            for _ in range(runs):
+                e0.record(stream)
+                launch()
+                e1.record(stream)
+                e1.synchronize()
+                tot += e0.elapsed_time(e1) * 1e-3
+            res[name] = tot / runs
+        results[str(bs)] = res
+        checks[str(bs)] = worst
+        del d, dy
+    if args.results_json:
+        with open(args.results_json, "w") as f:
+            json.dump(results, f, indent=2, sort_keys=True)
+    best = {bs: min((k for k in r if k != "CPU CSR"), key=r.get) for bs, r in results.items()}
+    print(json.dumps({"workload": f"ndiag {args.ndiag_dtype}: gen_n_diag_bcsr {n_rows} block rows x "
+                                  f"{blocks_per_row} blocks, bs {list(sizes)}, {runs} runs per format",
+                      "results": results, "fastest": best, "worst_compare_results": checks}), flush=True)
+
+
 def main():
     args = parse_args()
     if args.workload == "serve":
@@ -683,6 +765,9 @@ def main():
         return
     if args.workload == "batch":
         run_batch(args)
+        return
+    if args.workload == "ndiag":
+        run_ndiag(args)
         return
     if args.impl == "reference":
         run_reference(args)

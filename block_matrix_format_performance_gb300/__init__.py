@@ -211,6 +211,23 @@ def csr_spmv(variant, row_ptr, cols, vals, x, y, n_cols=None, stream=None):
     return y
 
 
+def bcsr_spmv_host(row_ptr, cols, vals, x, bs, y=None, n_block_cols=None, lanes=0, stream=None):
+    """y = A x with every array in host memory (numpy, ideally views of pinned
+    buffers) through bmfp_bcsr_spmv_host: chunked upload overlapped with the
+    product, result in y on return. bs = 1 multiplies CSR."""
+    vals = np.ascontiguousarray(vals).reshape(-1)
+    row_ptr, cols = _i32(row_ptr), _i32(cols)
+    x = np.ascontiguousarray(x, dtype=vals.dtype)
+    nbr = row_ptr.size - 1
+    if y is None:
+        y = np.empty(nbr * bs, dtype=vals.dtype)
+    assert y.dtype == vals.dtype and y.flags.c_contiguous and y.size == nbr * bs
+    nbc = n_block_cols if n_block_cols is not None else x.size // bs
+    check(load().bmfp_bcsr_spmv_host(dtype_enum(vals.dtype), nbr, nbc, bs, cols.size, _p(row_ptr), _p(cols),
+                                     _p(vals), _p(x), _p(y), lanes, _stream(stream)))
+    return y
+
+
 def native_default_lanes(dtype, bs, avg_blocks_per_row) -> int:
     return load().bmfp_bcsr_native_default_lanes(dtype_enum(dtype), bs, float(avg_blocks_per_row))
 

@@ -26,6 +26,7 @@ LIB = os.path.join(PKG, "libbmfp.so")
 SOURCES = [
     "spmv_native.cu",
     "spmv_variants.cu",
+    "spmv_host.cpp",
     "vector_ops.cu",
     "bicgstab.cu",
     "batch.cu",

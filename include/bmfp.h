@@ -157,6 +157,25 @@ BMFP_API int bmfp_bcsr_spmv_native_ex (int dtype, int n_block_rows, int bs, int6
                                        int lanes_per_block_row, void *stream);
 BMFP_API int bmfp_bcsr_native_default_lanes (int dtype, int bs, double avg_blocks_per_row);
 
+/* One-shot product on HOST buffers: y = A x with the BCSR arrays (row-major
+ * blocks; bs = 1 is CSR), x and y all in host memory, the call returning when
+ * h_y holds the result. Replaces what each gpu_bcsr_spmv / gpu_csr_spmv call
+ * of the reference does around its kernels (gpu/gpu_matrix_multiplier.cu:
+ * 106-115 and 757-766 allocate and upload, :151-156 download, :158-160 free)
+ * for callers that keep their matrices on the host. The upload is split into
+ * block-row chunks: the product of chunk k runs while chunk k+1 is still
+ * crossing the host link, so the call costs about one transfer of the
+ * arrays. Device memory comes from a stream-ordered pool private to the
+ * library that keeps up to 16 GiB per device for the next call. Pinned host
+ * buffers (cudaHostAlloc / cudaHostRegister) give full link speed; pageable
+ * ones work through the driver's staging copies. lanes as for
+ * bmfp_bcsr_spmv_native_ex (0 = built-in choice). stream: the stream the
+ * copies are ordered on (NULL = legacy default). */
+BMFP_API int bmfp_bcsr_spmv_host (int dtype, int n_block_rows, int n_block_cols, int bs,
+                                  int64_t nnzb, const int *h_row_ptr, const int *h_cols,
+                                  const void *h_values, const void *h_x, void *h_y, int lanes,
+                                  void *stream);
+
 /* ------------------------------------------------ device matrix handles ---
  * A device-resident BCSR (or CSR when bs is given as 0 to *_csr) matrix owned
  * by the library: one upload, then any number of products. The reference

@@ -227,3 +227,36 @@ def test_full_size_band_sweep_parity(lib, orc, cuda, bs, dtype):
     y_ref = orc.csr_spmv(crp, cc, cv, x, threads=8)
     assert np.all(np.abs(y - y_ref) <= spmv_tolerance(orc, crp, cc, cv, x, dtype))
     m.close()
+
+
+@pytest.mark.parametrize("bs,dtype,pinned", [(1, np.float64, True), (2, np.float64, True), (3, np.float64, False),
+                                             (4, np.float64, True), (8, np.float32, True), (32, np.float64, False),
+                                             (16, np.float32, False)])
+def test_host_buffer_spmv_chunked(lib, orc, cuda, bs, dtype, pinned):
+    """bmfp_bcsr_spmv_host: host arrays in, host y out, the upload split into
+    block-row chunks with the product of each chunk overlapping the next
+    upload. Sizes are picked so that most cases cut the matrix into several
+    chunks (8 MB each at least), including ragged rows and empty rows."""
+    import torch
+    nbr = 60_000 if bs <= 4 else 6_000
+    rp, c, v = ragged_bcsr(nbr, nbr, bs, seed=bs, dtype=dtype, max_blocks=16)
+    x = np.random.default_rng(bs).uniform(-1, 1, nbr * bs).astype(dtype)
+    if pinned:
+        pin = [torch.from_numpy(a).pin_memory() for a in (rp, c, v, x)]
+        rp, c, v, x = (t.numpy() for t in pin)
+    y = bm.bcsr_spmv_host(rp, c, v, x, bs)
+    crp, cc, cv = orc.bcsr_to_csr(rp, c, v, bs)
+    y_ref = orc.csr_spmv(crp, cc, cv, x, threads=8)
+    assert np.all(np.abs(y - y_ref) <= spmv_tolerance(orc, crp, cc, cv, x, dtype))
+    # repeated calls reuse the pooled device memory and give the same bits
+    assert np.array_equal(bm.bcsr_spmv_host(rp, c, v, x, bs).view(np.uint8), y.view(np.uint8))
+
+
+def test_host_buffer_spmv_edges(lib, orc, cuda):
+    # no rows, no blocks (y = 0), and a malformed row_ptr refused before any copy
+    assert bm.bcsr_spmv_host(np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0), np.zeros(0), 2).size == 0
+    y = bm.bcsr_spmv_host(np.zeros(5, np.int32), np.zeros(0, np.int32), np.zeros(0), np.ones(8), 2)
+    assert np.array_equal(y, np.zeros(8))
+    with pytest.raises(bm.BmfpError) as e:
+        bm.bcsr_spmv_host(np.array([0, 2], np.int32), np.zeros(1, np.int32), np.zeros(4), np.ones(2), 2)
+    assert e.value.status == bm.ERROR_INVALID_VALUE
