@@ -84,7 +84,7 @@ def parse_args():
     ap.add_argument("--requests", type=int, default=1000, help="serve: number of requests")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (req/s)")
     ap.add_argument("--grid", default="200x50", help="solve: nodes nx x ny of the Q4 grid")
-    ap.add_argument("--precision", default="fp64", choices=("fp64", "fp32", "mixed"))
+    ap.add_argument("--precision", default="fp64", choices=("fp64", "fp32", "mixed", "both"))
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--max-iters", type=int, default=200000)
     ap.add_argument("--repeats", type=int, default=3)
@@ -483,8 +483,10 @@ def run_reference(args):
 
 
 def run_solve(args):
-    """One Q4 plane-stress solve (the FEM workloads), timed end to end on the
-    device: solves/s, iterations, true residual and bytes per iteration."""
+    """Q4 plane-stress solves (the FEM workloads), timed end to end on the
+    device: solves/s, iterations, true residual and bytes per iteration.
+    --precision both runs plain FP64 and FP32-inner / FP64-refined on the same
+    system and reports the mixed solution's error against the FP64 one."""
     import torch
 
     import block_matrix_format_performance_gb300 as bm
@@ -493,24 +495,30 @@ def run_solve(args):
     nx, ny = (int(t) for t in args.grid.lower().split("x"))
     rp, c, v, rhs = bm.gen_q4_elasticity(nx, ny)
     A = bm.Matrix.from_bcsr(rp, c, v, 2)
-    s = bm.Solver(A, args.precision, tol=args.tol, max_iters=args.max_iters)
     d_b = torch.from_numpy(rhs).cuda()
-    d_x = torch.empty_like(d_b)
-    infos = []
-    for _ in range(max(1, args.repeats)):
-        infos.append(s.solve(d_b, d_x))
-    best = min(infos, key=lambda i: i["seconds"])
     n = 2 * nx * ny
-    spmv_b = bm.bcsr_spmv_bytes(np.float64 if args.precision == "fp64" else np.float32, nx * ny, nx * ny, 2,
-                                int(c.size))
-    per_iter = 2 * spmv_b + 17 * n * (8 if args.precision == "fp64" else 4)
-    it = max(best["iterations"], 1)
-    print(json.dumps({"workload": "solve", "grid": [nx, ny], "dofs": n, "nnzb": int(c.size),
-                      "precision": args.precision, "tol": args.tol, "solves_per_s": round(1.0 / best["seconds"], 3),
-                      "seconds": round(best["seconds"], 4), "us_per_iteration": round(best["seconds"] / it * 1e6, 2),
-                      "bytes_per_iteration": int(per_iter),
-                      "gbs_per_iteration": round(per_iter / (best["seconds"] / it) / 1e9, 1), **best}), flush=True)
-    s.close()
+    out, xs = {}, {}
+    for prec in (("fp64", "mixed") if args.precision == "both" else (args.precision,)):
+        s = bm.Solver(A, prec, tol=args.tol, max_iters=args.max_iters)
+        d_x = torch.empty_like(d_b)
+        infos = [s.solve(d_b, d_x) for _ in range(max(1, args.repeats))]
+        s.close()
+        best = min(infos, key=lambda i: i["seconds"])
+        xs[prec] = d_x
+        spmv_b = bm.bcsr_spmv_bytes(np.float64 if prec == "fp64" else np.float32, nx * ny, nx * ny, 2, int(c.size))
+        per_iter = 2 * spmv_b + 17 * n * (8 if prec == "fp64" else 4)
+        it = max(best["iterations"], 1)
+        out[prec] = {"solves_per_s": round(1.0 / best["seconds"], 3), "seconds": round(best["seconds"], 4),
+                     "us_per_iteration": round(best["seconds"] / it * 1e6, 2), "bytes_per_iteration": int(per_iter),
+                     "gbs_per_iteration": round(per_iter / (best["seconds"] / it) / 1e9, 1), **best}
+    line = {"workload": "solve", "grid": [nx, ny], "dofs": n, "nnzb": int(c.size), "tol": args.tol}
+    if len(out) == 1:
+        line.update(precision=args.precision, **out[args.precision])
+    else:
+        line.update(out)
+        ref = xs["fp64"].double()
+        line["mixed_error_vs_fp64"] = float(torch.linalg.norm(xs["mixed"].double() - ref) / torch.linalg.norm(ref))
+    print(json.dumps(line), flush=True)
     A.close()
 
 

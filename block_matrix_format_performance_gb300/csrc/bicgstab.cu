@@ -748,11 +748,27 @@ int WideEngine::start_residual (const void *d_r, double tol, int max_iter_total,
   return BMFP_SUCCESS;
 }
 
-int WideEngine::run (cudaStream_t s, DevState *out)
+namespace
+{
+// Stops a run from the host side: the phase kernels of the graphs still to
+// come see done and return at once.
+__global__ void stop_kernel (DevState *st)
+{
+  st->done = 1;
+  st->status = kStateBreakdown;
+}
+} // namespace
+
+int WideEngine::run (cudaStream_t s, DevState *out, void *d_snap, double *snap_rr)
 {
   // Keep one graph in flight while the host inspects the previous one.
   long k = 0;
   const long limit = 1 + (long) 1e9 / chunk_;
+  const size_t xbytes = dtype_size (dtype_) * (size_t) n_;
+  double best = INFINITY;                              // smallest (r, r) polled
+  double snap_at = snap_rr ? *snap_rr : INFINITY;      // (r, r) of the last copy
+  long snap_k = -1;                                    // graph whose end the copy holds
+  bool stopping = false;
   for (;; k++)
     {
       BMFP_CUDA (cudaGraphLaunch (graph_, s));
@@ -761,14 +777,34 @@ int WideEngine::run (cudaStream_t s, DevState *out)
       if (k > 0)
         {
           BMFP_CUDA (cudaEventSynchronize (ev_[(k - 1) & 1]));
-          if (h_state_[(k - 1) & 1].done)
+          const DevState &h = h_state_[(k - 1) & 1];
+          if (snap_k == k - 1)
+            *snap_rr = snap_at = h.rr;
+          if (h.done)
             break;
+          if (h.rr < best)
+            best = h.rr;
+          // x after graph k (queued behind it); its (r, r) is read next poll.
+          if (d_snap && snap_rr && h.rr < 0.25 * snap_at && snap_k != k - 1)
+            {
+              BMFP_CUDA (cudaMemcpyAsync (d_snap, x_, xbytes, cudaMemcpyDeviceToDevice, s));
+              snap_k = k;
+              snap_at = h.rr;
+            }
+          if (!stopping && !(h.rr <= 1e16 * best))
+            {
+              stop_kernel<<<1, 1, 0, s>>> (state_);
+              BMFP_LAUNCH_CHECK ();
+              stopping = true;
+            }
         }
       if (k > limit)
         return fail (BMFP_ERROR_TIMEOUT, "solver did not stop");
     }
   BMFP_CUDA (cudaStreamSynchronize (s));
   *out = h_state_[k & 1];
+  if (snap_k == k && snap_rr)
+    *snap_rr = out->rr;
   return BMFP_SUCCESS;
 }
 

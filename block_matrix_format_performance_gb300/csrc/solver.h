@@ -55,7 +55,12 @@ public:
   int start_residual (const void *d_r, double tol, int max_iter_total, double norm_b,
                       cudaStream_t stream);
   // Run graph chunks until the device sets done; returns the final state.
-  int run (cudaStream_t stream, DevState *out);
+  // Runs graphs until the device sets done. With d_snapshot, x is copied
+  // there each time the recursive residual has fallen 4x below the last copy
+  // (and below snapshot_rr on entry), and *snapshot_rr receives the (r, r) of
+  // the copy; a residual that grows 1e8-fold over the best seen, or turns
+  // non-finite, stops the run as a breakdown.
+  int run (cudaStream_t stream, DevState *out, void *d_snapshot = nullptr, double *snapshot_rr = nullptr);
   // r = b - A x, returns ||r||^2 and ||b||^2 (synchronises the stream).
   int true_residual (const void *d_b, void *d_r, double *rr, double *bb, cudaStream_t stream);
 

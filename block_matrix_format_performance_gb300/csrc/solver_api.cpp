@@ -20,6 +20,7 @@ struct bmfp_solver_s
   void *work_a = nullptr;               // residual / converted right-hand side
   void *work_b = nullptr;
   void *work_c = nullptr;               // best iterate kept across restarts
+  void *work_d = nullptr;               // best iterate within one run (WideEngine::run snapshot)
 
   ~bmfp_solver_s ()
   {
@@ -30,6 +31,7 @@ struct bmfp_solver_s
     cudaFree (work_a);
     cudaFree (work_b);
     cudaFree (work_c);
+    cudaFree (work_d);
   }
 };
 
@@ -44,15 +46,34 @@ int status_of (const DevState &st)
   return BMFP_ERROR_NOT_CONVERGED;
 }
 
+// Runs the engine and, when the run ends above the best point it passed (a
+// breakdown, a blow-up stopped by the engine, or the iteration limit reached
+// on an erratic stretch of the residual history), puts x back at that point.
+int run_keep_best (WideEngine &e, void *d_snap, DevState *st, cudaStream_t s)
+{
+  double snap_rr = INFINITY;
+  int rc = e.run (s, st, d_snap, &snap_rr);
+  if (rc != BMFP_SUCCESS)
+    return rc;
+  if (st->status != kStateConverged && snap_rr < INFINITY && !(st->rr <= snap_rr))
+    {
+      BMFP_CUDA (cudaMemcpyAsync (e.x (), d_snap, dtype_size (e.dtype ()) * (size_t) e.n (),
+                                  cudaMemcpyDeviceToDevice, s));
+      BMFP_CUDA (cudaStreamSynchronize (s));
+      st->rr = snap_rr;
+    }
+  return BMFP_SUCCESS;
+}
+
 // Restart loop shared by the plain and the mixed solves: verify b - A x,
 // restart from the true residual while each restart still lowers it (at most
 // 8 times), and keep the best iterate: near the attainable accuracy of the working
 // precision a restart can leave x worse (asking the recursive residual for
 // less than the tolerance only makes that more likely, measured), and then x
 // is restored.
-int finish_with_restarts (WideEngine &e, const void *d_b, void *d_r, void *d_xbest, const bmfp_solver_options &o,
-                          DevState &st, int iter_budget, double norm_b, int *restarts_out, double *rel_out,
-                          cudaStream_t s)
+int finish_with_restarts (WideEngine &e, const void *d_b, void *d_r, void *d_xbest, void *d_snap,
+                          const bmfp_solver_options &o, DevState &st, int iter_budget, double norm_b,
+                          int *restarts_out, double *rel_out, cudaStream_t s)
 {
   const size_t xbytes = dtype_size (e.dtype ()) * (size_t) e.n ();
   double best = INFINITY;
@@ -79,13 +100,15 @@ int finish_with_restarts (WideEngine &e, const void *d_b, void *d_r, void *d_xbe
         }
       best = rel;
       best_st = st;
-      if (rel < o.tolerance || st.status != kStateConverged || st.iter >= iter_budget || restarts >= 8)
+      // A breakdown also restarts (a fresh shadow residual is the usual
+      // cure); only the iteration limit ends the loop here.
+      if (rel < o.tolerance || st.status == kStateMaxIter || st.iter >= iter_budget || restarts >= 8)
         break;
       BMFP_CUDA (cudaMemcpyAsync (d_xbest, e.x (), xbytes, cudaMemcpyDeviceToDevice, s));
       restarts++;
       rc = e.start_residual (d_r, o.tolerance, iter_budget, norm_b > 0 ? norm_b : std::sqrt (bb), s);
       if (rc == BMFP_SUCCESS)
-        rc = e.run (s, &st);
+        rc = run_keep_best (e, d_snap, &st, s);
       if (rc != BMFP_SUCCESS)
         return rc;
     }
@@ -96,13 +119,13 @@ int finish_with_restarts (WideEngine &e, const void *d_b, void *d_r, void *d_xbe
 
 // Solve with one engine from x0 = 0, then (optionally) verify the true
 // residual and restart from it (finish_with_restarts).
-int solve_plain (WideEngine &e, const void *d_b, void *d_r, void *d_xbest, const bmfp_solver_options &o,
-                 bmfp_solve_info *info, cudaStream_t s)
+int solve_plain (WideEngine &e, const void *d_b, void *d_r, void *d_xbest, void *d_snap,
+                 const bmfp_solver_options &o, bmfp_solve_info *info, cudaStream_t s)
 {
   DevState st{};
   int rc = e.start_zero (d_b, o.tolerance, o.max_iterations, s);
   if (rc == BMFP_SUCCESS)
-    rc = e.run (s, &st);
+    rc = run_keep_best (e, d_snap, &st, s);
   if (rc != BMFP_SUCCESS)
     return rc;
   int status = status_of (st);
@@ -110,7 +133,8 @@ int solve_plain (WideEngine &e, const void *d_b, void *d_r, void *d_xbest, const
   int restarts = 0;
   if (o.check_true_residual)
     {
-      rc = finish_with_restarts (e, d_b, d_r, d_xbest, o, st, o.max_iterations, -1.0, &restarts, &rel_true, s);
+      rc = finish_with_restarts (e, d_b, d_r, d_xbest, d_snap, o, st, o.max_iterations, -1.0, &restarts, &rel_true,
+                                 s);
       if (rc != BMFP_SUCCESS)
         return rc;
       status = rel_true < o.tolerance ? BMFP_SUCCESS
@@ -163,13 +187,13 @@ int solve_mixed (bmfp_solver_s *sv, const void *d_b, bmfp_solve_info *info, cuda
           DevState st{};
           rc = e64.start_residual (r64, o.tolerance, o.max_iterations - iters32, std::sqrt (bb), s);
           if (rc == BMFP_SUCCESS)
-            rc = e64.run (s, &st);
+            rc = run_keep_best (e64, sv->work_d, &st, s);
           if (rc != BMFP_SUCCESS)
             return rc;
           int restarts = 0;
           double rel_fin = NAN;
-          rc = finish_with_restarts (e64, d_b, r64, sv->work_c, o, st, o.max_iterations - iters32, std::sqrt (bb),
-                                     &restarts, &rel_fin, s);
+          rc = finish_with_restarts (e64, d_b, r64, sv->work_c, sv->work_d, o, st, o.max_iterations - iters32,
+                                     std::sqrt (bb), &restarts, &rel_fin, s);
           if (rc != BMFP_SUCCESS)
             return rc;
           iters64 = st.iter;
@@ -292,6 +316,7 @@ int bmfp_solver_create (bmfp_solver_t *out, bmfp_matrix_t A, const bmfp_solver_o
   BMFP_CUDA (cudaMalloc (&sv->work_a, nb * 8));
   BMFP_CUDA (cudaMalloc (&sv->work_b, nb * 8));
   BMFP_CUDA (cudaMalloc (&sv->work_c, nb * 8));
+  BMFP_CUDA (cudaMalloc (&sv->work_d, nb * 8));
   *out = sv.release ();
   return BMFP_SUCCESS;
 }
@@ -323,7 +348,7 @@ int bmfp_solver_solve (bmfp_solver_t sv, const void *d_b, void *d_x, bmfp_solve_
           b = sv->work_b;
         }
       if (rc == BMFP_SUCCESS)
-        rc = solve_plain (e, b, sv->work_a, sv->work_c, sv->opts, &info, s);
+        rc = solve_plain (e, b, sv->work_a, sv->work_c, sv->work_d, sv->opts, &info, s);
       if (e.dtype () == BMFP_R32F)
         info.iterations_fp32 = info.iterations;
       if (rc == BMFP_SUCCESS)
