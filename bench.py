@@ -290,12 +290,18 @@ def run_ours(args):
     t_max = max_over_ranks(step_ms, dist, "cuda")
     value = replica_value(total_bytes, world, t_max * 1e-3)
 
+    # The second roofline of FP64 products: GB300's FP64 FMA rate, measured
+    # here (one FMA per value, so at most bytes / (2 nnzb bs^2 / rate)).
+    fp64_gflops = bm.measure_fma_peak(np.float64)
     per_case = {}
     for i, cs in enumerate(cases):
         ms = per_case_ms[i] / args.steps
-        per_case[f"bs{cs['bs']}_{cs['tag']}"] = {"gbs": round(cs["bytes"] / (ms * 1e-3) / 1e9, 1),
-                                                  "us": round(ms * 1e3, 2), "mb": round(cs["bytes"] / 1e6, 1),
-                                                  "lanes": cs["lanes"]}
+        gbs = cs["bytes"] / (ms * 1e-3) / 1e9
+        per_case[f"bs{cs['bs']}_{cs['tag']}"] = {"gbs": round(gbs, 1), "us": round(ms * 1e3, 2),
+                                                  "mb": round(cs["bytes"] / 1e6, 1), "lanes": cs["lanes"]}
+        if cs["tag"] == "f64":
+            bound = cs["bytes"] / (2.0 * cs["nnzb"] * cs["bs"] ** 2 / (fp64_gflops * 1e9)) / 1e9
+            per_case[f"bs{cs['bs']}_{cs['tag']}"]["of_min_hbm_fp64_bound"] = round(gbs / min(bound, peaks()[0]), 3)
     dom = max(range(n), key=lambda i: per_case_ms[i])
     dcs = cases[dom]
     dom_ms = per_case_ms[dom] / args.steps
@@ -303,6 +309,13 @@ def run_ours(args):
     achieved = dcs["bytes"] / (dom_ms * 1e-3) / 1e9
     dom_key = f"bcsr_native_bs{dcs['bs']}_{dcs['tag']}"
     traffic = committed_traffic(dom_key)
+    fp64_bound = None
+    if dcs["tag"] == "f64":
+        flops = 2.0 * dcs["nnzb"] * dcs["bs"] ** 2
+        bound_gbs = dcs["bytes"] / (flops / (fp64_gflops * 1e9)) / 1e9
+        fp64_bound = {"fp64_fma_gflops_measured": round(fp64_gflops, 1), "bound_gbs": round(bound_gbs, 1),
+                      "frac": round(achieved / bound_gbs, 4),
+                      "binding": "fp64_pipe" if bound_gbs < hbm else "hbm"}
 
     # CSR warp-per-row ("GPU CSR-Vector") on the same matrices, for comparison.
     csr_cmp = {}
@@ -387,7 +400,7 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": dom_key, "achieved": round(achieved, 1), "peak": hbm,
                      "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                      else "fallback 6.8 TB/s", "unit": "GB/s", "frac": round(achieved / hbm, 4),
-                     "traffic": traffic, "algorithmic_bytes": dcs["bytes"]},
+                     "traffic": traffic, "algorithmic_bytes": dcs["bytes"], "fp64_pipe": fp64_bound},
         "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "s_per_step": round(e2e_s, 4)},
         "gpu_launches": args.steps * n,

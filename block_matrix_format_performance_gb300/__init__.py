@@ -228,6 +228,13 @@ def bcsr_spmv_host(row_ptr, cols, vals, x, bs, y=None, n_block_cols=None, lanes=
     return y
 
 
+def measure_fma_peak(dtype=np.float64, stream=None) -> float:
+    """FMA throughput of the current GPU in GFLOP/s (bmfp_measure_fma_peak)."""
+    g = ctypes.c_double()
+    check(load().bmfp_measure_fma_peak(dtype_enum(dtype), ctypes.byref(g), _stream(stream)))
+    return g.value
+
+
 def native_default_lanes(dtype, bs, avg_blocks_per_row) -> int:
     return load().bmfp_bcsr_native_default_lanes(dtype_enum(dtype), bs, float(avg_blocks_per_row))
 

@@ -27,6 +27,7 @@ SOURCES = [
     "spmv_native.cu",
     "spmv_variants.cu",
     "spmv_host.cpp",
+    "peaks.cu",
     "vector_ops.cu",
     "bicgstab.cu",
     "batch.cu",

@@ -157,6 +157,12 @@ BMFP_API int bmfp_bcsr_spmv_native_ex (int dtype, int n_block_rows, int bs, int6
                                        int lanes_per_block_row, void *stream);
 BMFP_API int bmfp_bcsr_native_default_lanes (int dtype, int bs, double avg_blocks_per_row);
 
+/* Measured FMA throughput of the current device in GFLOP/s (2 flop per FMA)
+ * for dtype R64F or R32F: a few milliseconds of independent FMA chains on
+ * every SM. FP64 sparse products are bound by it on GB300 (one FMA per value,
+ * so at most 4 bytes per FP64 flop); bench.py reports both rooflines. */
+BMFP_API int bmfp_measure_fma_peak (int dtype, double *gflops, void *stream);
+
 /* One-shot product on HOST buffers: y = A x with the BCSR arrays (row-major
  * blocks; bs = 1 is CSR), x and y all in host memory, the call returning when
  * h_y holds the result. Replaces what each gpu_bcsr_spmv / gpu_csr_spmv call

@@ -54,3 +54,11 @@ def test_batch_workload_line(cuda):
     line = run_bench("--workload", "batch", "--systems", "8", "--repeats", "1")
     assert line["systems"] == 8 and "fp64" in line and line["fp64"]["solves_per_s"] > 0
     assert "per_request_fp64" in line
+
+
+def test_fma_peak_probe(cuda):
+    import block_matrix_format_performance_gb300 as bm
+    import numpy as np
+    f64 = bm.measure_fma_peak(np.float64)
+    f32 = bm.measure_fma_peak(np.float32)
+    assert 50.0 < f64 < f32  # GFLOP/s; FP32 FMA is far faster than FP64 on GB300
