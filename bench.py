@@ -81,13 +81,19 @@ def parse_args():
     ap.add_argument("--ndiag-rows", type=int, default=50_000, help="ndiag: block rows")
     ap.add_argument("--ndiag-dtype", default="f32", choices=("f32", "f64"))
     ap.add_argument("--systems", type=int, default=256, help="batch: number of systems")
+    ap.add_argument("--batch-grid", default=None, help="batch: one NXxNY grid for every system (default: uneven)")
     ap.add_argument("--requests", type=int, default=1000, help="serve: number of requests")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (req/s)")
+    ap.add_argument("--wide-lanes", type=int, default=None, help="serve: concurrent whole-GPU solves")
+    ap.add_argument("--wide-threshold", type=int, default=None, help="serve: rows from which a request "
+                                                                          "takes a whole-GPU lane")
+    ap.add_argument("--no-baseline", action="store_true", help="serve: skip the FIFO per-request baseline")
     ap.add_argument("--grid", default="200x50", help="solve: nodes nx x ny of the Q4 grid")
     ap.add_argument("--precision", default="fp64", choices=("fp64", "fp32", "mixed", "both"))
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--max-iters", type=int, default=200000)
     ap.add_argument("--repeats", type=int, default=3)
+    ap.add_argument("--ctas-per-sm", type=int, default=0, help="solve: persistent grid of the solver (0 = default)")
     return ap.parse_args()
 
 
@@ -512,7 +518,8 @@ def run_solve(args):
     n = 2 * nx * ny
     out, xs = {}, {}
     for prec in (("fp64", "mixed") if args.precision == "both" else (args.precision,)):
-        s = bm.Solver(A, prec, tol=args.tol, max_iters=args.max_iters)
+        kw = {"ctas_per_sm": args.ctas_per_sm} if args.ctas_per_sm else {}
+        s = bm.Solver(A, prec, tol=args.tol, max_iters=args.max_iters, **kw)
         d_x = torch.empty_like(d_b)
         infos = [s.solve(d_b, d_x) for _ in range(max(1, args.repeats))]
         s.close()
@@ -542,14 +549,14 @@ def batch_grids(n_systems, seed=0):
     return [(int(nx), max(2, int(round(nx / 4)))) for nx in nxs]
 
 
-def measure_batch(precisions, tol, max_iters, repeats, n_systems=256, per_request=True):
+def measure_batch(precisions, tol, max_iters, repeats, n_systems=256, per_request=True, grid=None):
     """The uneven batch (nx log-uniform in [20, 400], ny = nx / 4, seeded): each
     precision solved by one persistent, graph-captured launch, and the plain
     FP64 per-request solver run system after system on the same GPU."""
     import torch
 
     import block_matrix_format_performance_gb300 as bm
-    grids = batch_grids(n_systems)
+    grids = batch_grids(n_systems) if grid is None else [grid] * n_systems
     mats, rhs = [], []
     for nx, ny in grids:
         rp, c, v, b = bm.gen_q4_elasticity(nx, ny)
@@ -599,8 +606,9 @@ def measure_batch(precisions, tol, max_iters, repeats, n_systems=256, per_reques
 def run_batch(args):
     from block_matrix_format_performance_gb300 import build as B
     B.build()
+    grid = tuple(int(t) for t in args.batch_grid.lower().split("x")) if args.batch_grid else None
     res = measure_batch([args.precision], args.tol, args.max_iters, args.repeats, args.systems,
-                        per_request=args.repeats > 0)
+                        per_request=args.repeats > 0, grid=grid)
     print(json.dumps({"workload": "batch", "precision": args.precision, **res}), flush=True)
 
 
@@ -637,7 +645,12 @@ def run_serve(args):
         b.reshape(ny, nx, 2)[:, 0, :] = 0.0  # clamped column carries no load
         rhs.append(b)
     xs = [np.zeros_like(b) for b in rhs]
-    srv = bm.Server(args.precision, tol=args.tol, max_iters=args.max_iters)
+    kw = {}
+    if args.wide_lanes is not None:
+        kw["wide_lanes"] = args.wide_lanes
+    if args.wide_threshold is not None:
+        kw["wide_threshold_rows"] = args.wide_threshold
+    srv = bm.Server(args.precision, tol=args.tol, max_iters=args.max_iters, **kw)
     # warm-up: one small request
     w = np.zeros(mats[min(mats)].rows)
     srv.wait(srv.submit(mats[min(mats)], np.ones_like(w), w))
@@ -659,6 +672,7 @@ def run_serve(args):
         infos.append(srv.wait(t))
     makespan = time.perf_counter() - t_start
     stats = srv.stats()
+    srv_opts = {"wide_lanes": srv.options.wide_lanes, "wide_threshold_rows": srv.options.wide_threshold_rows}
     srv.close()
     lat = np.array([i["seconds"] for i in infos])
     conv = sum(i["status"] == 0 for i in infos)
@@ -667,6 +681,8 @@ def run_serve(args):
     # the queue is replayed with those service times.
     solvers, service_by_grid = {}, {}
     for k, g in enumerate(grids):
+        if args.no_baseline:
+            break
         if g in service_by_grid:
             continue
         s = bm.Solver(mats[g], "fp64", tol=args.tol, max_iters=args.max_iters)
@@ -678,10 +694,18 @@ def run_serve(args):
         s.close()
     done, base_lat = 0.0, []
     for k, g in enumerate(grids):
+        if args.no_baseline:
+            break
         done = max(done, arrivals[k]) + service_by_grid[g]
         base_lat.append(done - arrivals[k])
     base_tput = len(grids) / max(done, 1e-9)
     nb = len(grids)
+    baseline = None if args.no_baseline else {
+        "requests": nb, "distinct_grids_timed": len(service_by_grid), "solves_per_s": round(base_tput, 2),
+        "latency_p50_s": round(float(np.percentile(base_lat, 50)), 4),
+        "latency_p99_s": round(float(np.percentile(base_lat, 99)), 4)}
+    bad = [{"grid": list(grids[k]), "status": i["status"], "true_rel": i["true_rel_residual"]}
+           for k, i in enumerate(infos) if i["status"] != 0][:12]
     print(json.dumps({
         "workload": "serve", "requests": len(grids), "rate_req_s": args.rate, "precision": args.precision,
         "tol": args.tol, "large_requests": int(sum(g == (1000, 250) for g in grids)),
@@ -689,11 +713,9 @@ def run_serve(args):
         "latency_p50_s": round(float(np.percentile(lat, 50)), 4), "latency_p99_s": round(float(np.percentile(lat, 99)), 4),
         "converged": conv, "worst_true_rel": max(i["true_rel_residual"] for i in infos),
         "micro_batches": stats["micro_batches"], "wide_solves": stats["wide_solves"],
-        "peak_device_bytes": stats["peak_bytes"],
-        "per_request_fp64": {"requests": nb, "distinct_grids_timed": len(service_by_grid),
-                             "solves_per_s": round(base_tput, 2),
-                             "latency_p50_s": round(float(np.percentile(base_lat, 50)), 4),
-                             "latency_p99_s": round(float(np.percentile(base_lat, 99)), 4)}}), flush=True)
+        "peak_device_bytes": stats["peak_bytes"], "wide_lanes": srv_opts["wide_lanes"],
+        "wide_threshold_rows": srv_opts["wide_threshold_rows"], "not_converged": bad,
+        "per_request_fp64": baseline}), flush=True)
 
 
 def run_ndiag(args, sizes=(2, 4, 8, 16, 32), blocks_per_row=6, runs=10):

@@ -202,9 +202,16 @@ struct Scal
 // One BiCGStab solve by the team. r0 = rhs (x updated in place from x0 = 0
 // when zero_x, else from the given x with rhs its residual). Stops when
 // ||r|| < tol * norm_ref (norm_ref <= 0: ||rhs||).
+//
+// With snap (FP64 runs), x is copied there whenever the recursive residual
+// has fallen 4x below the last copy, and a run that ends above that point
+// (breakdown, iteration limit) returns it; a residual that grows 1e8-fold
+// over the best seen, or turns non-finite, ends the run as a breakdown. Each
+// thread copies and restores the elements it also updates, so the copies
+// need no barrier of their own.
 template <typename T, int OP>
 __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, const T *rhs, T *x, bool zero_x,
-                                   double tol, int max_it, double norm_ref)
+                                   double tol, int max_it, double norm_ref, T *snap = nullptr)
 {
   using Op = TeamOp<T, OP>;
   const TeamIdx ix = team_index<Op::G> (cl);
@@ -230,8 +237,18 @@ __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, c
   const double nb = sc.a;
   double rho = out1[0], rr = out1[0]; // rh == r at the start
   double rho_prev = 1.0, alpha = 1.0, omega = 1.0;
+  // Team-uniform (every thread holds the same rr), so no broadcast needed.
+  double best_rr = rr, snap_rr = INFINITY;
   for (;;)
     {
+      if (rr < best_rr)
+        best_rr = rr;
+      if (snap && rr < 0.25 * snap_rr)
+        {
+          for (int64_t i = ix.elem0; i < S.n; i += ix.elem_stride)
+            snap[i] = x[i];
+          snap_rr = rr;
+        }
       // convergence, limits and beta (gpu/bicgstab.cu:451, :512)
       __syncthreads ();
       if (threadIdx.x == 0)
@@ -242,7 +259,7 @@ __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, c
             st = 1;
           else if (o.iters >= max_it)
             st = 2;
-          else if (rho == 0.0 || omega == 0.0 || !isfinite (rho))
+          else if (rho == 0.0 || omega == 0.0 || !isfinite (rho) || !(rr <= 1e16 * best_rr))
             st = 3;
           else
             {
@@ -321,6 +338,12 @@ __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, c
       rr = nx[1];
       o.iters++;
     }
+  if (snap && o.status != 1 && snap_rr < INFINITY && !(rr <= snap_rr))
+    {
+      for (int64_t i = ix.elem0; i < S.n; i += ix.elem_stride)
+        x[i] = snap[i];
+      o.rec_rel = nb > 0.0 ? sqrt (snap_rr) / nb : 0.0;
+    }
   cl.sync (); // x, r complete before anyone reads them
   return o;
 }
@@ -359,12 +382,13 @@ __device__ Fp64Result fp64_restarted (cg::cluster_group &cl, const TeamSys<doubl
   __shared__ double sh_rel, sh_nb;
   const TeamIdx ix = team_index<1> (cl);
   double *xb = D.w64 + 7 * D.n;
+  double *snap = D.w64 + 8 * D.n;
   Fp64Result f;
   double best = INFINITY;
   for (;;)
     {
       const SolveOut o = team_bicgstab<double, OP> (cl, S64, first ? D.b : r64, D.x, first, P.tol, budget - f.iters,
-                                                    norm_b);
+                                                    norm_b, snap);
       f.iters += o.iters;
       double rr, bb;
       team_residual<OP> (cl, S64, D.b, D.x, r64, rr, bb);
@@ -397,7 +421,9 @@ __device__ Fp64Result fp64_restarted (cg::cluster_group &cl, const TeamSys<doubl
       f.rel = rel;
       f.status = o.status;
       f.rec = o.rec_rel;
-      if (rel < P.tol || o.status != 1 || f.iters >= budget || f.restarts >= 8)
+      // A breakdown restarts too (fresh shadow residual); the iteration
+      // limit ends the loop.
+      if (rel < P.tol || o.status == 2 || f.iters >= budget || f.restarts >= 8)
         break;
       for (int64_t i = ix.elem0; i < D.n; i += ix.elem_stride)
         xb[i] = D.x[i];
@@ -657,7 +683,7 @@ int BatchEngine::init (int n, const bmfp_matrix_s *const *mats, const bmfp_solve
       total += rows[i];
     }
   const bool lowp = o.precision != BMFP_SOLVE_FP64;
-  BMFP_CUDA (cudaMalloc (&w64_, sizeof (double) * (size_t) std::max<int64_t> (8 * total, 1)));
+  BMFP_CUDA (cudaMalloc (&w64_, sizeof (double) * (size_t) std::max<int64_t> (9 * total, 1)));
   if (lowp)
     BMFP_CUDA (cudaMalloc (&w32_, sizeof (float) * (size_t) std::max<int64_t> (8 * total, 1)));
   BMFP_CUDA (cudaMallocHost (&h_desc_, sizeof (BatchDesc) * (size_t) std::max (n, 1)));
@@ -683,7 +709,7 @@ int BatchEngine::init (int n, const bmfp_matrix_s *const *mats, const bmfp_solve
         op_ = D.op;
       else if (op_ != D.op)
         op_ = kOpTpr; // mixed block sizes: the generic warp-per-block-row routine
-      D.w64 = (double *) w64_ + 8 * off;
+      D.w64 = (double *) w64_ + 9 * off;
       D.w32 = lowp ? (float *) w32_ + 8 * off : nullptr;
       D.vals32 = nullptr;
       if (lowp)

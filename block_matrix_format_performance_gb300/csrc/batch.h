@@ -17,7 +17,7 @@ struct BatchDesc
   const float *vals32 = nullptr;
   const double *b = nullptr;
   double *x = nullptr;
-  double *w64 = nullptr; // 8 n: r, rh, p, v, s, t, residual, best x
+  double *w64 = nullptr; // 9 n: r, rh, p, v, s, t, residual, best x, in-run snapshot
   float *w32 = nullptr;  // 8 n: r, rh, p, v, s, t, x32, rhs32
 };
 

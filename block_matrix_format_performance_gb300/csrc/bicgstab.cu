@@ -250,7 +250,7 @@ __global__ void __launch_bounds__ (kThreads)
 // Fresh start (ZERO: x = 0, r = b) or restart from a given true residual.
 template <typename T, bool ZERO>
 __global__ void __launch_bounds__ (kThreads)
-  start_kernel (Args<T> a, const T *src, double tol, int max_iter, double norm_b)
+  start_kernel (Args<T> a, const T *src, double tol, int max_iter, double norm_b, int iter0)
 {
   double rr = 0.0;
   GRID_STRIDE (i, a.n)
@@ -283,8 +283,13 @@ __global__ void __launch_bounds__ (kThreads)
           st->iter = 0;
           st->norm_b = -1.0; // set from the first phase-1 sum
         }
-      else if (norm_b > 0.0)
-        st->norm_b = norm_b;
+      else
+        {
+          if (norm_b > 0.0)
+            st->norm_b = norm_b;
+          if (iter0 >= 0)
+            st->iter = iter0;
+        }
     }
 }
 
@@ -342,13 +347,36 @@ __global__ void __launch_bounds__ (kThreads) phase_p (Args<T> a)
   if (sh_status != kStateRunning)
     return;
   const T tb = (T) sh_beta, tw = (T) sh_omega;
-  GRID_STRIDE (i, a.n)
-  {
-    const T pn = a.r[i] + tb * (a.p[i] - tw * a.v[i]); // :286-304
-    a.p[i] = pn;
-    if (PRE)
-      a.q[i] = a.P[i] * pn; // :227-238
-  }
+  // Four grid-stride elements per pass, loads first (the arrays may alias as
+  // far as the compiler knows, so it would not hoist them itself).
+  const int64_t stride = (int64_t) gridDim.x * blockDim.x;
+  int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < a.n; i += 4 * stride)
+    {
+      T rv[4], pv[4], vv[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        {
+          rv[u] = a.r[i + u * stride];
+          pv[u] = a.p[i + u * stride];
+          vv[u] = a.v[i + u * stride];
+        }
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        {
+          const T pn = rv[u] + tb * (pv[u] - tw * vv[u]); // :286-304
+          a.p[i + u * stride] = pn;
+          if (PRE)
+            a.q[i + u * stride] = a.P[i + u * stride] * pn; // :227-238
+        }
+    }
+  for (; i < a.n; i += stride)
+    {
+      const T pn = a.r[i] + tb * (a.p[i] - tw * a.v[i]);
+      a.p[i] = pn;
+      if (PRE)
+        a.q[i] = a.P[i] * pn;
+    }
 }
 
 // phase 3
@@ -387,13 +415,33 @@ __global__ void __launch_bounds__ (kThreads) phase_s (Args<T> a)
   if (!isfinite (alpha))
     return;
   const T ta = (T) alpha;
-  GRID_STRIDE (i, a.n)
-  {
-    const T si = a.r[i] - ta * a.v[i]; // :306-327
-    a.s[i] = si;
-    if (PRE)
-      a.z[i] = a.P[i] * si;
-  }
+  const int64_t stride = (int64_t) gridDim.x * blockDim.x;
+  int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < a.n; i += 4 * stride)
+    {
+      T rv[4], vv[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        {
+          rv[u] = a.r[i + u * stride];
+          vv[u] = a.v[i + u * stride];
+        }
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        {
+          const T si = rv[u] - ta * vv[u]; // :306-327
+          a.s[i + u * stride] = si;
+          if (PRE)
+            a.z[i + u * stride] = a.P[i + u * stride] * si;
+        }
+    }
+  for (; i < a.n; i += stride)
+    {
+      const T si = a.r[i] - ta * a.v[i];
+      a.s[i] = si;
+      if (PRE)
+        a.z[i] = a.P[i] * si;
+    }
 }
 
 // phase 5
@@ -425,16 +473,44 @@ __global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
     return;
   const T ta = (T) sh_alpha, tw = (T) omega;
   double rhr = 0.0, rr = 0.0;
-  GRID_STRIDE (i, a.n)
-  {
-    const T qi = PRE ? a.q[i] : a.p[i];
-    const T zi = PRE ? a.z[i] : a.s[i];
-    a.x[i] = a.x[i] + ta * qi + tw * zi;     // h = x + alpha q; x = h + omega z
-    const T ri = a.s[i] - tw * a.t[i];       // :340-357
-    a.r[i] = ri;
-    rhr = fma ((double) a.rh[i], (double) ri, rhr);
-    rr = fma ((double) ri, (double) ri, rr);
-  }
+  const T *qa = PRE ? a.q : a.p;
+  const T *za = PRE ? a.z : a.s;
+  const int64_t stride = (int64_t) gridDim.x * blockDim.x;
+  int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < a.n; i += 4 * stride)
+    {
+      T xv[4], qv[4], zv[4], sv[4], tv[4], hv[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        {
+          const int64_t k = i + u * stride;
+          xv[u] = a.x[k];
+          qv[u] = qa[k];
+          zv[u] = za[k];
+          sv[u] = a.s[k];
+          tv[u] = a.t[k];
+          hv[u] = a.rh[k];
+        }
+      // Same per-thread accumulation order as one element at a time.
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        {
+          const int64_t k = i + u * stride;
+          a.x[k] = xv[u] + ta * qv[u] + tw * zv[u]; // h = x + alpha q; x = h + omega z
+          const T ri = sv[u] - tw * tv[u];           // :340-357
+          a.r[k] = ri;
+          rhr = fma ((double) hv[u], (double) ri, rhr);
+          rr = fma ((double) ri, (double) ri, rr);
+        }
+    }
+  for (; i < a.n; i += stride)
+    {
+      a.x[i] = a.x[i] + ta * qa[i] + tw * za[i];
+      const T ri = a.s[i] - tw * a.t[i];
+      a.r[i] = ri;
+      rhr = fma ((double) a.rh[i], (double) ri, rhr);
+      rr = fma ((double) ri, (double) ri, rr);
+    }
   double vals[2] = { rhr, rr };
   const int kk[2] = { kRhR, kRR };
   store_parts<2> (vals, a.part, a.grid, kk);
@@ -607,7 +683,7 @@ WideEngine::~WideEngine ()
     cudaFreeHost (h_state_);
 }
 
-int WideEngine::init (const bmfp_matrix_s *A, bool jacobi, int chunk, cudaStream_t stream)
+int WideEngine::init (const bmfp_matrix_s *A, bool jacobi, int chunk, cudaStream_t stream, int ctas_per_sm)
 {
   if (!A)
     return fail (BMFP_ERROR_INVALID_VALUE, "null matrix");
@@ -628,7 +704,7 @@ int WideEngine::init (const bmfp_matrix_s *A, bool jacobi, int chunk, cudaStream
   BMFP_CUDA (cudaDeviceGetAttribute (&sms, cudaDevAttrMultiProcessorCount, dev));
   // Persistent grid: a few CTAs per SM, never more than the rows need.
   const int64_t want = std::max<int64_t> (1, (n_ + kThreads - 1) / kThreads);
-  grid_ = (int) std::min<int64_t> ((int64_t) sms * 4, want);
+  grid_ = (int) std::min<int64_t> ((int64_t) sms * std::max (1, std::min (ctas_per_sm, 8)), want);
   const size_t S = dtype_size (dtype_);
   const size_t vb = S * (size_t) std::max<int64_t> (n_, 1);
   for (void **ptr : { &x_, &r_, &rh_, &p_, &v_, &s_, &t_ })
@@ -722,28 +798,28 @@ int WideEngine::start_zero (const void *d_b, double tol, int max_iter, cudaStrea
   if (dtype_ == BMFP_R64F)
     start_kernel<double, true><<<grid_, kThreads, 0, s>>> (
       make_args<double> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, part_, grid_, state_),
-      (const double *) d_b, tol, max_iter, -1.0);
+      (const double *) d_b, tol, max_iter, -1.0, 0);
   else
     start_kernel<float, true><<<grid_, kThreads, 0, s>>> (
       make_args<float> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, part_, grid_, state_),
-      (const float *) d_b, tol, max_iter, -1.0);
+      (const float *) d_b, tol, max_iter, -1.0, 0);
   BMFP_LAUNCH_CHECK ();
   return BMFP_SUCCESS;
 }
 
 int WideEngine::start_residual (const void *d_r, double tol, int max_iter_total, double norm_b,
-                                cudaStream_t s)
+                                cudaStream_t s, int iter0)
 {
   void *q = jacobi_ ? q_ : p_;
   void *z = jacobi_ ? z_ : s_;
   if (dtype_ == BMFP_R64F)
     start_kernel<double, false><<<grid_, kThreads, 0, s>>> (
       make_args<double> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, part_, grid_, state_),
-      (const double *) d_r, tol, max_iter_total, norm_b);
+      (const double *) d_r, tol, max_iter_total, norm_b, iter0);
   else
     start_kernel<float, false><<<grid_, kThreads, 0, s>>> (
       make_args<float> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, part_, grid_, state_),
-      (const float *) d_r, tol, max_iter_total, norm_b);
+      (const float *) d_r, tol, max_iter_total, norm_b, iter0);
   BMFP_LAUNCH_CHECK ();
   return BMFP_SUCCESS;
 }
@@ -889,10 +965,10 @@ int raw_start (const RawSolve &b, const void *d_rhs, double tol, int max_iter, c
 {
   if (b.A.dtype == BMFP_R64F)
     start_kernel<double, true><<<b.grid, kThreads, 0, s>>> (raw_args<double> (b), (const double *) d_rhs,
-                                                            tol, max_iter, -1.0);
+                                                            tol, max_iter, -1.0, 0);
   else
     start_kernel<float, true><<<b.grid, kThreads, 0, s>>> (raw_args<float> (b), (const float *) d_rhs,
-                                                           tol, max_iter, -1.0);
+                                                           tol, max_iter, -1.0, 0);
   BMFP_LAUNCH_CHECK ();
   return BMFP_SUCCESS;
 }

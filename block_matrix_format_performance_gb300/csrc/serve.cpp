@@ -99,8 +99,8 @@ namespace
 size_t request_bytes (const bmfp_server_s *sv, int64_t n, bool wide)
 {
   if (wide)
-    return (size_t) n * 8 * 14; // solver vectors (work and Krylov) + b, x
-  size_t b = align256 (n * 8) * 2 + align256 (n * 8 * 8); // b, x, 8 FP64 work vectors
+    return (size_t) n * 8 * 15; // solver vectors (work and Krylov) + b, x
+  size_t b = align256 (n * 8) * 2 + align256 (n * 8 * 9); // b, x, 9 FP64 work vectors
   if (sv->opts.solver.precision != BMFP_SOLVE_FP64)
     b += align256 (n * 4 * 8); // 8 FP32 work vectors
   return b;
@@ -167,7 +167,7 @@ int launch_micro_batch (bmfp_server_s *sv, std::vector<Request *> &reqs)
       r->d_x = (double *) p;
       p += align256 (r->n * 8);
       r->w64 = (double *) p;
-      p += align256 (r->n * 8 * 8);
+      p += align256 (r->n * 8 * 9);
       if (sv->opts.solver.precision != BMFP_SOLVE_FP64)
         {
           r->w32 = (float *) p;

@@ -46,14 +46,16 @@ public:
   WideEngine (const WideEngine &) = delete;
   WideEngine &operator= (const WideEngine &) = delete;
 
-  int init (const bmfp_matrix_s *A, bool jacobi, int chunk, cudaStream_t stream);
+  int init (const bmfp_matrix_s *A, bool jacobi, int chunk, cudaStream_t stream, int ctas_per_sm = 4);
   // Start a solve of A x = b from x0 = 0 (b on the device, engine dtype).
   int start_zero (const void *d_b, double tol, int max_iter, cudaStream_t stream);
   // Restart from the current x with the residual given in d_r (true residual).
   // norm_b > 0 sets the reference norm of the convergence test (an engine that
   // never ran start_zero has none); norm_b <= 0 keeps the previous one.
+  // iter0 >= 0 restarts the iteration count there (a new solve on an engine
+  // whose last run belonged to an earlier one); -1 keeps counting.
   int start_residual (const void *d_r, double tol, int max_iter_total, double norm_b,
-                      cudaStream_t stream);
+                      cudaStream_t stream, int iter0 = -1);
   // Run graph chunks until the device sets done; returns the final state.
   // Runs graphs until the device sets done. With d_snapshot, x is copied
   // there each time the recursive residual has fallen 4x below the last copy

@@ -185,7 +185,9 @@ int solve_mixed (bmfp_solver_s *sv, const void *d_b, bmfp_solve_info *info, cuda
           // Finish in FP64 from the current x (restart from its true residual).
           info->used_fp64_fallback = 1;
           DevState st{};
-          rc = e64.start_residual (r64, o.tolerance, o.max_iterations - iters32, std::sqrt (bb), s);
+          // A fresh count: this engine's device counter still holds the
+          // last run of an earlier solve on the same solver.
+          rc = e64.start_residual (r64, o.tolerance, o.max_iterations - iters32, std::sqrt (bb), s, 0);
           if (rc == BMFP_SUCCESS)
             rc = run_keep_best (e64, sv->work_d, &st, s);
           if (rc != BMFP_SUCCESS)
@@ -203,6 +205,31 @@ int solve_mixed (bmfp_solver_s *sv, const void *d_b, bmfp_solve_info *info, cuda
                                                : (st.status == kStateBreakdown ? BMFP_ERROR_BREAKDOWN
                                                                                : BMFP_ERROR_NOT_CONVERGED);
           info->restarts += restarts;
+          if (info->status == BMFP_ERROR_BREAKDOWN && iters32 + iters64 < o.max_iterations)
+            {
+              // BiCGStab from the refined iterate can break down again and
+              // again (its residual makes a poor shadow vector there, measured
+              // on an elasticity system that plain FP64 solves from x = 0).
+              // Solve from x = 0 with the budget left and keep the better x.
+              const size_t xb = sizeof (double) * (size_t) n;
+              BMFP_CUDA (cudaMemcpyAsync (sv->work_b, e64.x (), xb, cudaMemcpyDeviceToDevice, s));
+              bmfp_solver_options o2 = o;
+              o2.max_iterations = o.max_iterations - iters32 - iters64;
+              bmfp_solve_info i2{};
+              rc = solve_plain (e64, d_b, r64, sv->work_c, sv->work_d, o2, &i2, s);
+              if (rc != BMFP_SUCCESS)
+                return rc;
+              iters64 += i2.iterations;
+              info->restarts += i2.restarts;
+              if (i2.true_rel_residual < rel_fin)
+                {
+                  info->true_rel_residual = i2.true_rel_residual;
+                  info->recursive_rel_residual = i2.recursive_rel_residual;
+                  info->status = i2.status;
+                }
+              else
+                BMFP_CUDA (cudaMemcpyAsync (e64.x (), sv->work_b, xb, cudaMemcpyDeviceToDevice, s));
+            }
           break;
         }
       prev_rel = rel;
@@ -253,6 +280,7 @@ void bmfp_solver_options_init (bmfp_solver_options *o)
   o->max_refinements = 30;
   o->fallback_fp64 = 1;
   o->iterations_per_graph = 16;
+  o->ctas_per_sm = 4;
 }
 
 int bmfp_solver_create (bmfp_solver_t *out, bmfp_matrix_t A, const bmfp_solver_options *opts,
@@ -269,7 +297,8 @@ int bmfp_solver_create (bmfp_solver_t *out, bmfp_matrix_t A, const bmfp_solver_o
     return fail (BMFP_ERROR_INVALID_VALUE, "invalid precision %d", o.precision);
   if (o.preconditioner != BMFP_PRECOND_NONE && o.preconditioner != BMFP_PRECOND_JACOBI)
     return fail (BMFP_ERROR_INVALID_VALUE, "invalid preconditioner %d", o.preconditioner);
-  if (!(o.tolerance > 0) || o.max_iterations < 0 || o.iterations_per_graph < 1)
+  if (!(o.tolerance > 0) || o.max_iterations < 0 || o.iterations_per_graph < 1 || o.ctas_per_sm < 1
+      || o.ctas_per_sm > 8)
     return fail (BMFP_ERROR_INVALID_VALUE, "invalid tolerance or iteration limits");
   if (o.precision == BMFP_SOLVE_MIXED && A->dtype != BMFP_R64F)
     return fail (BMFP_ERROR_INVALID_VALUE, "mixed precision needs an FP64 matrix");
@@ -298,16 +327,16 @@ int bmfp_solver_create (bmfp_solver_t *out, bmfp_matrix_t A, const bmfp_solver_o
   if (o.precision == BMFP_SOLVE_FP32)
     {
       sv->main.reset (new (std::nothrow) WideEngine);
-      rc = sv->main->init (A32, jac, o.iterations_per_graph, s);
+      rc = sv->main->init (A32, jac, o.iterations_per_graph, s, o.ctas_per_sm);
     }
   else
     {
       sv->main.reset (new (std::nothrow) WideEngine);
-      rc = sv->main->init (A, jac, o.iterations_per_graph, s);
+      rc = sv->main->init (A, jac, o.iterations_per_graph, s, o.ctas_per_sm);
       if (rc == BMFP_SUCCESS && o.precision == BMFP_SOLVE_MIXED)
         {
           sv->inner.reset (new (std::nothrow) WideEngine);
-          rc = sv->inner->init (A32, jac, o.iterations_per_graph, s);
+          rc = sv->inner->init (A32, jac, o.iterations_per_graph, s, o.ctas_per_sm);
         }
     }
   if (rc != BMFP_SUCCESS)

@@ -42,14 +42,20 @@ __device__ __forceinline__ void flat_row (int row, const int *__restrict__ row_p
 
   if constexpr (CH >= E)
     {
+      // Whole groups of U chunks first, with no predicates, then one chunk at
+      // a time for the rest: a row of 9 blocks costs 9 block steps rather
+      // than 12 (every warp-wide FP64 instruction is paid in full on GB300,
+      // active lanes or not). The per-lane accumulation order is the block
+      // order either way.
       constexpr int BPI = CH / E;
       const int bl = (gl * V) / E;
       const int o = (gl * V) % E;
+      int b0 = 0;
       if constexpr (V <= BS)
         {
           const int c0 = o % BS;
           T acc = 0;
-          for (int b0 = 0; b0 < nblk; b0 += BPI * U)
+          for (; b0 + BPI * U <= nblk; b0 += BPI * U)
             {
               V16 a[U];
               int c[U];
@@ -57,22 +63,29 @@ __device__ __forceinline__ void flat_row (int row, const int *__restrict__ row_p
               for (int u = 0; u < U; u++)
                 {
                   const int b = b0 + u * BPI + bl;
-                  c[u] = -1;
-                  if (b < nblk)
-                    {
-                      a[u] = dev::ld_stream16 (vb + b * E + o);
-                      c[u] = __ldg (cb + b);
-                    }
+                  a[u] = dev::ld_stream16 (vb + b * E + o);
+                  c[u] = __ldg (cb + b);
                 }
 #pragma unroll
               for (int u = 0; u < U; u++)
-                if (c[u] >= 0)
-                  {
-                    const V16 xv = dev::ld_cached16 (x + (size_t) c[u] * BS + c0);
+                {
+                  const V16 xv = dev::ld_cached16 (x + (size_t) c[u] * BS + c0);
 #pragma unroll
-                    for (int v = 0; v < V; v++)
-                      acc = fma (a[u].v[v], xv.v[v], acc);
-                  }
+                  for (int v = 0; v < V; v++)
+                    acc = fma (a[u].v[v], xv.v[v], acc);
+                }
+            }
+          for (; b0 < nblk; b0 += BPI)
+            {
+              const int b = b0 + bl;
+              if (b < nblk)
+                {
+                  const V16 av = dev::ld_stream16 (vb + b * E + o);
+                  const V16 xv = dev::ld_cached16 (x + (size_t) __ldg (cb + b) * BS + c0);
+#pragma unroll
+                  for (int v = 0; v < V; v++)
+                    acc = fma (av.v[v], xv.v[v], acc);
+                }
             }
 #pragma unroll
           for (int off = 1; off < BS / V; off <<= 1)
@@ -91,7 +104,7 @@ __device__ __forceinline__ void flat_row (int row, const int *__restrict__ row_p
         {
           static_assert (V == E, "unexpected vector/block shape");
           T acc0 = 0, acc1 = 0;
-          for (int b0 = 0; b0 < nblk; b0 += BPI * U)
+          for (; b0 + BPI * U <= nblk; b0 += BPI * U)
             {
               V16 a[U];
               int c[U];
@@ -99,24 +112,33 @@ __device__ __forceinline__ void flat_row (int row, const int *__restrict__ row_p
               for (int u = 0; u < U; u++)
                 {
                   const int b = b0 + u * BPI + bl;
-                  c[u] = -1;
-                  if (b < nblk)
-                    {
-                      a[u] = dev::ld_stream16 (vb + b * E);
-                      c[u] = __ldg (cb + b);
-                    }
+                  a[u] = dev::ld_stream16 (vb + b * E);
+                  c[u] = __ldg (cb + b);
                 }
 #pragma unroll
               for (int u = 0; u < U; u++)
-                if (c[u] >= 0)
-                  {
-                    T x0, x1;
-                    dev::ld_cached2 (x + (size_t) c[u] * 2, x0, x1);
-                    acc0 = fma (a[u].v[0], x0, acc0);
-                    acc0 = fma (a[u].v[1], x1, acc0);
-                    acc1 = fma (a[u].v[2], x0, acc1);
-                    acc1 = fma (a[u].v[3], x1, acc1);
-                  }
+                {
+                  T x0, x1;
+                  dev::ld_cached2 (x + (size_t) c[u] * 2, x0, x1);
+                  acc0 = fma (a[u].v[0], x0, acc0);
+                  acc0 = fma (a[u].v[1], x1, acc0);
+                  acc1 = fma (a[u].v[2], x0, acc1);
+                  acc1 = fma (a[u].v[3], x1, acc1);
+                }
+            }
+          for (; b0 < nblk; b0 += BPI)
+            {
+              const int b = b0 + bl;
+              if (b < nblk)
+                {
+                  const V16 av = dev::ld_stream16 (vb + b * E);
+                  T x0, x1;
+                  dev::ld_cached2 (x + (size_t) __ldg (cb + b) * 2, x0, x1);
+                  acc0 = fma (av.v[0], x0, acc0);
+                  acc0 = fma (av.v[1], x1, acc0);
+                  acc1 = fma (av.v[2], x0, acc1);
+                  acc1 = fma (av.v[3], x1, acc1);
+                }
             }
           acc0 = dev::group_sum<G> (acc0);
           acc1 = dev::group_sum<G> (acc1);

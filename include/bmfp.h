@@ -263,6 +263,9 @@ typedef struct bmfp_solver_options
   int fallback_fp64;        /* MIXED: when an outer step cuts the FP64 residual by less
                                than 4x, finish with FP64 BiCGStab from the current x */
   int iterations_per_graph; /* BiCGStab iterations per CUDA graph launch */
+  int ctas_per_sm;          /* persistent grid of the single-system solver: CTAs of 256
+                               threads per SM (default 4); the grid fixes the summation
+                               order, so results are bitwise repeatable for a given value */
 } bmfp_solver_options;
 
 typedef struct bmfp_solve_info

@@ -151,6 +151,27 @@ def test_mixed_precision_ill_conditioned_falls_back_and_converges(lib, cuda):
     assert np.linalg.norm(rhs - K @ x) / np.linalg.norm(rhs) < 1e-10
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_reused_solver_gives_the_same_answer_every_time(lib, cuda, precision):
+    """A solver object serves many right-hand sides (the server's whole-GPU
+    lanes keep one per matrix): nothing of an earlier solve may leak into the
+    next. Mixed precision on this grid ends in the FP64 finish, which once
+    kept counting iterations across solves until the limit stopped it at x = 0."""
+    rp, c, v, rhs = bm.gen_q4_elasticity(100, 25)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    K = bcsr_dense_csr(rp, c, v, 2)
+    s = bm.Solver(A, precision, tol=1e-10, max_iters=3000)
+    rng = np.random.default_rng(5)
+    bs = [rhs, rng.uniform(-1, 1, rhs.size), rhs]
+    out = [s.solve_host(b) for b in bs]
+    for (x, info), b in zip(out, bs):
+        assert info["status"] == bm.SUCCESS, info
+        assert info["iterations"] <= 3000
+        assert np.linalg.norm(b - K @ x) / np.linalg.norm(b) < 1e-10
+    assert np.array_equal(out[0][0].view(np.uint64), out[2][0].view(np.uint64))
+    assert out[0][1]["iterations"] == out[2][1]["iterations"]
+
+
 def test_zero_rhs_and_iteration_limit(lib, cuda):
     rp, c, v, rhs = bm.gen_q4_elasticity(30, 8)
     A = bm.Matrix.from_bcsr(rp, c, v, 2)
@@ -171,3 +192,28 @@ def test_solver_rejects_bad_configurations(lib, cuda):
     rect = bm.Matrix.from_bcsr(rp, c, v, 2, n_block_cols=12)
     with pytest.raises(bm.BmfpError):
         bm.Solver(rect, "fp64")
+
+
+def test_mixed_finish_that_breaks_down_restarts_from_zero(lib, cuda):
+    """Request 729 of the seeded serving stream (1000x250 elasticity grid,
+    random load): FP64 BiCGStab started from the FP32-refined iterate breaks
+    down again and again there, while plain FP64 from x = 0 converges. The
+    mixed solver must then solve from x = 0 and reach plain FP64's result."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    _, grids = bench.serve_stream(1000, 2000.0)
+    rng = np.random.default_rng(7)
+    b = None
+    for k, (nx, ny) in enumerate(grids[:730]):
+        b = rng.uniform(-1, 1, 2 * nx * ny)
+        b.reshape(ny, nx, 2)[:, 0, :] = 0.0
+    assert grids[729] == (1000, 250)
+    rp, c, v, _ = bm.gen_q4_elasticity(1000, 250)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    x64, i64 = bm.Solver(A, "fp64", tol=1e-10).solve_host(b)
+    xm, im = bm.Solver(A, "mixed", tol=1e-10).solve_host(b)
+    assert i64["true_rel_residual"] < 1e-10
+    assert im["used_fp64_fallback"] == 1
+    assert im["true_rel_residual"] <= max(1e-10, 2 * i64["true_rel_residual"]), im
