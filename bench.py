@@ -88,6 +88,7 @@ def parse_args():
     ap.add_argument("--wide-threshold", type=int, default=None, help="serve: rows from which a request "
                                                                           "takes a whole-GPU lane")
     ap.add_argument("--no-baseline", action="store_true", help="serve: skip the FIFO per-request baseline")
+    ap.add_argument("--large-fraction", type=float, default=0.05, help="serve: share of 1000x250 requests")
     ap.add_argument("--grid", default="200x50", help="solve: nodes nx x ny of the Q4 grid")
     ap.add_argument("--precision", default="fp64", choices=("fp64", "fp32", "mixed", "both"))
     ap.add_argument("--tol", type=float, default=1e-10)
@@ -612,13 +613,13 @@ def run_batch(args):
     print(json.dumps({"workload": "batch", "precision": args.precision, **res}), flush=True)
 
 
-def serve_stream(n_requests, rate, seed=1):
+def serve_stream(n_requests, rate, seed=1, large_fraction=0.05):
     """Seeded request stream: Poisson arrivals, grids as the uneven batch plus
     5 % 1000 x 250, right-hand sides uniform in [-1, 1) (0 on clamped DOFs)."""
     rng = np.random.default_rng(seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, n_requests))
     nxs = np.round(np.exp(rng.uniform(np.log(20), np.log(400), n_requests))).astype(int)
-    big = rng.random(n_requests) < 0.05
+    big = rng.random(n_requests) < large_fraction
     grids = [(1000, 250) if bg else (int(nx), max(2, int(round(nx / 4)))) for nx, bg in zip(nxs, big)]
     return arrivals, grids
 
@@ -633,7 +634,7 @@ def run_serve(args):
     import block_matrix_format_performance_gb300 as bm
     from block_matrix_format_performance_gb300 import build as B
     B.build()
-    arrivals, grids = serve_stream(args.requests, args.rate)
+    arrivals, grids = serve_stream(args.requests, args.rate, large_fraction=args.large_fraction)
     mats = {}
     for g in sorted(set(grids)):
         rp, c, v, _ = bm.gen_q4_elasticity(*g)

@@ -61,12 +61,59 @@ struct MicroBatch
   int stream = 0;
   void *d_mem = nullptr;
   size_t bytes = 0;
-  BatchDesc *h_desc = nullptr; // pinned
-  BatchOut *h_out = nullptr;   // pinned
+  char *h_slab = nullptr; // pinned staging from the server's pool
+  size_t h_cap = 0;
+  BatchDesc *h_desc = nullptr;
+  BatchOut *h_out = nullptr;
+  std::vector<double *> h_x; // pinned copies of each request's x
   cudaEvent_t done = nullptr;
 };
 
 size_t align256 (size_t b) { return (b + 255) & ~(size_t) 255; }
+
+// Page-locked staging buffers, recycled. Allocating or freeing page-locked
+// memory (like device memory) on the host serialises the streams of the
+// device, which would undo the overlap of micro-batches, so buffers are kept
+// and handed out again; new ones are only made while the pool grows.
+class PinnedPool
+{
+public:
+  // Caller holds the server lock.
+  char *take (size_t bytes, size_t *cap)
+  {
+    auto it = free_.lower_bound (bytes);
+    if (it != free_.end ())
+      {
+        char *p = it->second;
+        *cap = it->first;
+        free_.erase (it);
+        return p;
+      }
+    size_t c = 64 << 10;
+    while (c < bytes)
+      c <<= 1;
+    void *p = nullptr;
+    if (cudaMallocHost (&p, c) != cudaSuccess)
+      return nullptr;
+    all_.push_back (p);
+    *cap = c;
+    return (char *) p;
+  }
+  void give (char *p, size_t cap)
+  {
+    if (p)
+      free_.emplace (cap, p);
+  }
+  ~PinnedPool ()
+  {
+    for (void *p : all_)
+      cudaFreeHost (p);
+  }
+
+private:
+  std::multimap<size_t, char *> free_;
+  std::vector<void *> all_;
+};
 } // namespace
 
 struct bmfp_server_s
@@ -82,7 +129,10 @@ struct bmfp_server_s
   std::map<const bmfp_matrix_s *, void *> vals32; // FP32 copies for mixed / FP32 serving
   std::map<std::pair<int, const bmfp_matrix_s *>, bmfp_solver_t> wide_solvers; // per (lane, matrix)
   std::vector<cudaStream_t> streams;
+  std::vector<char> stream_busy;       // a micro-batch runs on the stream
   std::vector<cudaStream_t> wide_streams;
+  PinnedPool pinned;                   // staging for micro-batches (lock held)
+  cudaMemPool_t pool = nullptr;        // device memory of requests, stream-ordered
   size_t bytes_in_use = 0, peak_bytes = 0;
   int in_flight = 0;
   uint64_t next_ticket = 1, submitted = 0, completed = 0, micro_batches = 0, wide_solves = 0;
@@ -112,13 +162,13 @@ int ensure_vals32 (bmfp_server_s *sv, const bmfp_matrix_s *A, cudaStream_t s)
     return BMFP_SUCCESS;
   const int64_t nv = A->bs ? A->nnz * A->bs * A->bs : A->nnz;
   void *p = nullptr;
-  BMFP_CUDA (cudaMalloc (&p, sizeof (float) * (size_t) std::max<int64_t> (nv, 1)));
+  BMFP_CUDA (cudaMallocFromPoolAsync (&p, sizeof (float) * (size_t) std::max<int64_t> (nv, 1), sv->pool, s));
   int rc = convert_values (BMFP_R64F, BMFP_R32F, nv, A->d_vals, p, s);
   if (rc == BMFP_SUCCESS && cudaStreamSynchronize (s) != cudaSuccess)
     rc = BMFP_ERROR_CUDA; // other streams read the copy next
   if (rc != BMFP_SUCCESS)
     {
-      cudaFree (p);
+      cudaFreeAsync (p, s);
       return rc;
     }
   sv->vals32[A] = p;
@@ -135,20 +185,37 @@ void finish (bmfp_server_s *sv, Request *r)
 
 // Launch one micro-batch (called with the lock held; the device work is
 // asynchronous on the chosen stream).
-int launch_micro_batch (bmfp_server_s *sv, std::vector<Request *> &reqs)
+int launch_micro_batch (bmfp_server_s *sv, std::vector<Request *> &reqs, int stream)
 {
   std::unique_ptr<MicroBatch> mb (new MicroBatch);
   mb->reqs = reqs;
-  mb->stream = (int) (sv->micro_batches % sv->streams.size ());
+  mb->stream = stream;
   cudaStream_t s = sv->streams[mb->stream];
   const int n = (int) reqs.size ();
   size_t total = align256 (sizeof (BatchDesc) * n) + align256 (sizeof (BatchOut) * n) + 256 + align256 (sizeof (int) * n);
   for (Request *r : reqs)
     total += r->bytes;
-  BMFP_CUDA (cudaMallocAsync (&mb->d_mem, total, s));
+  BMFP_CUDA (cudaMallocFromPoolAsync (&mb->d_mem, total, sv->pool, s));
   mb->bytes = total;
-  BMFP_CUDA (cudaMallocHost (&mb->h_desc, sizeof (BatchDesc) * n));
-  BMFP_CUDA (cudaMallocHost (&mb->h_out, sizeof (BatchOut) * n));
+  // Pinned staging: descriptors, results, launch order, then b and x of
+  // every request (x comes back here and is copied out on retirement).
+  size_t hbytes = align256 (sizeof (BatchDesc) * n) + align256 (sizeof (BatchOut) * n) + align256 (sizeof (int) * n);
+  for (Request *r : reqs)
+    hbytes += 2 * align256 (sizeof (double) * r->n);
+  mb->h_slab = sv->pinned.take (hbytes, &mb->h_cap);
+  if (!mb->h_slab)
+    {
+      cudaFreeAsync (mb->d_mem, s);
+      return fail (BMFP_ERROR_OUT_OF_MEMORY, "page-locked staging of %zu bytes failed", hbytes);
+    }
+  char *hp = mb->h_slab;
+  mb->h_desc = (BatchDesc *) hp;
+  hp += align256 (sizeof (BatchDesc) * n);
+  mb->h_out = (BatchOut *) hp;
+  hp += align256 (sizeof (BatchOut) * n);
+  int *h_order = (int *) hp;
+  hp += align256 (sizeof (int) * n);
+  mb->h_x.resize (n);
   char *p = (char *) mb->d_mem;
   BatchDesc *d_desc = (BatchDesc *) p;
   p += align256 (sizeof (BatchDesc) * n);
@@ -161,6 +228,11 @@ int launch_micro_batch (bmfp_server_s *sv, std::vector<Request *> &reqs)
   std::vector<int> order (n);
   for (int i = 0; i < n; i++)
     {
+      double *h_b = (double *) hp;
+      hp += align256 (sizeof (double) * reqs[i]->n);
+      mb->h_x[i] = (double *) hp;
+      hp += align256 (sizeof (double) * reqs[i]->n);
+      std::memcpy (h_b, reqs[i]->b.data (), sizeof (double) * reqs[i]->n);
       Request *r = reqs[i];
       r->d_b = (double *) p;
       p += align256 (r->n * 8);
@@ -173,7 +245,7 @@ int launch_micro_batch (bmfp_server_s *sv, std::vector<Request *> &reqs)
           r->w32 = (float *) p;
           p += align256 (r->n * 4 * 8);
         }
-      BMFP_CUDA (cudaMemcpyAsync (r->d_b, r->b.data (), sizeof (double) * r->n, cudaMemcpyHostToDevice, s));
+      BMFP_CUDA (cudaMemcpyAsync (r->d_b, h_b, sizeof (double) * r->n, cudaMemcpyHostToDevice, s));
       BatchDesc &D = mb->h_desc[i];
       const bmfp_matrix_s *A = r->A;
       D.nbr = A->n_rows;
@@ -191,8 +263,9 @@ int launch_micro_batch (bmfp_server_s *sv, std::vector<Request *> &reqs)
       order[i] = i;
     }
   std::stable_sort (order.begin (), order.end (), [&] (int a, int b) { return reqs[a]->n > reqs[b]->n; });
+  std::memcpy (h_order, order.data (), sizeof (int) * n);
   BMFP_CUDA (cudaMemcpyAsync (d_desc, mb->h_desc, sizeof (BatchDesc) * n, cudaMemcpyHostToDevice, s));
-  BMFP_CUDA (cudaMemcpyAsync (d_order, order.data (), sizeof (int) * n, cudaMemcpyHostToDevice, s));
+  BMFP_CUDA (cudaMemcpyAsync (d_order, h_order, sizeof (int) * n, cudaMemcpyHostToDevice, s));
   BMFP_CUDA (cudaMemsetAsync (d_counter, 0, sizeof (int), s));
   BatchParams P;
   P.n_systems = n;
@@ -214,11 +287,15 @@ int launch_micro_batch (bmfp_server_s *sv, std::vector<Request *> &reqs)
   if (rc != BMFP_SUCCESS)
     return rc;
   BMFP_CUDA (cudaMemcpyAsync (mb->h_out, d_out, sizeof (BatchOut) * n, cudaMemcpyDeviceToHost, s));
+  for (int i = 0; i < n; i++)
+    if (reqs[i]->h_x)
+      BMFP_CUDA (cudaMemcpyAsync (mb->h_x[i], reqs[i]->d_x, sizeof (double) * reqs[i]->n, cudaMemcpyDeviceToHost, s));
   BMFP_CUDA (cudaEventCreateWithFlags (&mb->done, cudaEventDisableTiming));
   BMFP_CUDA (cudaEventRecord (mb->done, s));
   for (Request *r : reqs)
     r->info.status = BMFP_PENDING;
   sv->micro_batches++;
+  sv->stream_busy[stream] = 1;
   sv->running.push_back (std::move (mb));
   return BMFP_SUCCESS;
 }
@@ -243,7 +320,7 @@ bool retire (bmfp_server_s *sv)
           Request *r = mb->reqs[i];
           const BatchOut &o = mb->h_out[i];
           if (q == cudaSuccess && r->h_x)
-            cudaMemcpy (r->h_x, r->d_x, sizeof (double) * r->n, cudaMemcpyDeviceToHost);
+            std::memcpy (r->h_x, mb->h_x[i], sizeof (double) * r->n);
           bmfp_solve_info &f = r->info;
           f.status = q != cudaSuccess ? BMFP_ERROR_CUDA
                                       : (o.status == 1 ? BMFP_SUCCESS
@@ -260,9 +337,9 @@ bool retire (bmfp_server_s *sv)
           finish (sv, r);
         }
       cudaFreeAsync (mb->d_mem, sv->streams[mb->stream]);
+      sv->stream_busy[mb->stream] = 0;
       cudaEventDestroy (mb->done);
-      cudaFreeHost (mb->h_desc);
-      cudaFreeHost (mb->h_out);
+      sv->pinned.give (mb->h_slab, mb->h_cap);
       sv->running.erase (sv->running.begin () + k);
       any = true;
     }
@@ -277,16 +354,41 @@ void dispatcher_main (bmfp_server_s *sv)
     {
       if (retire (sv))
         sv->cv_done.notify_all ();
-      // Admit in arrival order while budget and slots allow.
+      // Admit in arrival order while budget and slots allow. A micro-batch
+      // starts only on an idle stream; while every stream is busy, arrivals
+      // wait and the next launch takes up to max_batch of them at once (one
+      // largest-first work queue for its teams). Light load thus gets a launch
+      // per request; heavy load gets large batches, which keep the teams
+      // busy from one system to the next. Whole-GPU requests do not wait for
+      // micro-batch streams.
       std::vector<Request *> admitted;
-      while (!sv->pending.empty ())
+      auto free_stream = [&] () {
+        for (size_t k = 0; k < sv->stream_busy.size (); k++)
+          if (!sv->stream_busy[k])
+            return (int) k;
+        return -1;
+      };
+      int slot = free_stream ();
+      bool blocked = false; // budget or in-flight limit reached: keep arrival order
+      for (auto it = sv->pending.begin (); it != sv->pending.end () && !blocked;)
         {
-          Request *r = sv->pending.front ();
+          Request *r = *it;
+          if (!r->wide && slot < 0)
+            {
+              ++it;
+              continue;
+            }
           if (sv->bytes_in_use + r->bytes > sv->opts.hbm_budget_bytes || sv->in_flight >= sv->opts.max_in_flight)
-            break;
+            {
+              blocked = true;
+              break;
+            }
           if (!r->wide && ensure_vals32 (sv, r->A, sv->streams[0]) != BMFP_SUCCESS)
-            break;
-          sv->pending.pop_front ();
+            {
+              blocked = true;
+              break;
+            }
+          it = sv->pending.erase (it);
           sv->bytes_in_use += r->bytes;
           sv->peak_bytes = std::max (sv->peak_bytes, sv->bytes_in_use);
           sv->in_flight++;
@@ -299,12 +401,13 @@ void dispatcher_main (bmfp_server_s *sv)
           admitted.push_back (r);
           if ((int) admitted.size () >= sv->opts.max_batch)
             {
-              if (launch_micro_batch (sv, admitted) != BMFP_SUCCESS && sv->error == BMFP_SUCCESS)
+              if (launch_micro_batch (sv, admitted, slot) != BMFP_SUCCESS && sv->error == BMFP_SUCCESS)
                 sv->error = BMFP_ERROR_CUDA;
               admitted.clear ();
+              slot = free_stream ();
             }
         }
-      if (!admitted.empty () && launch_micro_batch (sv, admitted) != BMFP_SUCCESS && sv->error == BMFP_SUCCESS)
+      if (!admitted.empty () && launch_micro_batch (sv, admitted, slot) != BMFP_SUCCESS && sv->error == BMFP_SUCCESS)
         sv->error = BMFP_ERROR_CUDA;
       if (sv->stop && sv->pending.empty () && sv->running.empty () && sv->in_flight == 0)
         break;
@@ -321,6 +424,10 @@ void wide_main (bmfp_server_s *sv, int lane)
 {
   cudaSetDevice (sv->device);
   cudaStream_t stream = sv->wide_streams[lane];
+  // This lane's page-locked staging for b and x, grown when a larger request
+  // comes (allocating page-locked memory serialises the device's streams).
+  double *h_stage = nullptr;
+  int64_t stage_n = 0;
   std::unique_lock<std::mutex> lk (sv->mu);
   for (;;)
     {
@@ -343,21 +450,39 @@ void wide_main (bmfp_server_s *sv, int lane)
       else
         solver = it->second;
       lk.unlock ();
-      double *d_b = nullptr, *d_x = nullptr;
-      if (rc == BMFP_SUCCESS && (cudaMalloc (&d_b, sizeof (double) * r->n) != cudaSuccess
-                                 || cudaMalloc (&d_x, sizeof (double) * r->n) != cudaSuccess))
+      if (rc == BMFP_SUCCESS && stage_n < r->n)
+        {
+          if (h_stage)
+            cudaFreeHost (h_stage);
+          h_stage = nullptr;
+          stage_n = 0;
+          if (cudaMallocHost (&h_stage, sizeof (double) * (size_t) r->n) == cudaSuccess)
+            stage_n = r->n;
+          else
+            rc = BMFP_ERROR_OUT_OF_MEMORY;
+        }
+      double *d_bx = nullptr; // b then x, from the server's stream-ordered pool
+      if (rc == BMFP_SUCCESS
+          && cudaMallocFromPoolAsync ((void **) &d_bx, 2 * sizeof (double) * (size_t) r->n, sv->pool, stream)
+               != cudaSuccess)
         rc = BMFP_ERROR_OUT_OF_MEMORY;
       if (rc == BMFP_SUCCESS)
         {
-          cudaMemcpyAsync (d_b, r->b.data (), sizeof (double) * r->n, cudaMemcpyHostToDevice, stream);
+          double *d_b = d_bx, *d_x = d_bx + r->n;
+          std::memcpy (h_stage, r->b.data (), sizeof (double) * r->n);
+          cudaMemcpyAsync (d_b, h_stage, sizeof (double) * r->n, cudaMemcpyHostToDevice, stream);
           rc = bmfp_solver_solve (solver, d_b, d_x, &r->info, stream);
           if (r->h_x)
-            cudaMemcpy (r->h_x, d_x, sizeof (double) * r->n, cudaMemcpyDeviceToHost);
+            {
+              cudaMemcpyAsync (h_stage, d_x, sizeof (double) * r->n, cudaMemcpyDeviceToHost, stream);
+              cudaStreamSynchronize (stream);
+              std::memcpy (r->h_x, h_stage, sizeof (double) * r->n);
+            }
         }
       else
         r->info.status = rc;
-      cudaFree (d_b);
-      cudaFree (d_x);
+      if (d_bx)
+        cudaFreeAsync (d_bx, stream);
       lk.lock ();
       sv->bytes_in_use -= r->bytes;
       sv->in_flight--;
@@ -366,6 +491,10 @@ void wide_main (bmfp_server_s *sv, int lane)
       sv->cv_done.notify_all ();
       sv->cv_work.notify_all ();
     }
+  lk.unlock ();
+  cudaStreamSynchronize (stream);
+  if (h_stage)
+    cudaFreeHost (h_stage);
 }
 } // namespace
 
@@ -378,9 +507,12 @@ void bmfp_server_options_init (bmfp_server_options *o)
   o->hbm_budget_bytes = (size_t) 120 << 30;
   o->max_in_flight = 4096;
   o->max_batch = 64;
-  o->streams = 48;
+  // Eight concurrent micro-batches: under load each later launch gathers up
+  // to max_batch waiting requests. Teams of 4 CTAs x 512 threads: the
+  // batched solver's autotuned choice on GB300 for uneven elasticity batches.
+  o->streams = 8;
   o->cluster_size = 4;
-  o->threads_per_cta = 256;
+  o->threads_per_cta = 512;
   // Above 200 000 rows a 4-CTA team takes tens of milliseconds per iteration
   // and can wander to the iteration cap (measured on 500 000-row elasticity
   // requests); the whole-GPU engine finishes them in about 0.35 s.
@@ -408,7 +540,20 @@ int bmfp_server_create (bmfp_server_t *out, const bmfp_server_options *opts)
     return fail (BMFP_ERROR_OUT_OF_MEMORY, "host allocation failed");
   sv->opts = o;
   BMFP_CUDA (cudaGetDevice (&sv->device));
+  {
+    // Requests' device memory comes from a pool of the server's own, kept
+    // (up to the HBM budget) between requests: no cudaMalloc / cudaFree, which
+    // would serialise the device's streams, on the serving path.
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = sv->device;
+    BMFP_CUDA (cudaMemPoolCreate (&sv->pool, &props));
+    uint64_t keep = (uint64_t) o.hbm_budget_bytes;
+    BMFP_CUDA (cudaMemPoolSetAttribute (sv->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  }
   sv->streams.resize (o.streams);
+  sv->stream_busy.assign (o.streams, 0);
   for (auto &s : sv->streams)
     BMFP_CUDA (cudaStreamCreateWithFlags (&s, cudaStreamNonBlocking));
   sv->wide_streams.resize (o.wide_lanes);
@@ -544,14 +689,19 @@ int bmfp_server_destroy (bmfp_server_t sv)
   for (auto &kv : sv->wide_solvers)
     bmfp_solver_destroy (kv.second);
   for (auto &kv : sv->vals32)
-    cudaFree (kv.second);
+    cudaFreeAsync (kv.second, sv->streams[0]);
   for (auto s : sv->streams)
     {
       cudaStreamSynchronize (s);
       cudaStreamDestroy (s);
     }
   for (auto s : sv->wide_streams)
-    cudaStreamDestroy (s);
+    {
+      cudaStreamSynchronize (s);
+      cudaStreamDestroy (s);
+    }
+  if (sv->pool)
+    cudaMemPoolDestroy (sv->pool);
   delete sv;
   return BMFP_SUCCESS;
 }

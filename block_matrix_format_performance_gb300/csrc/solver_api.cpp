@@ -21,6 +21,7 @@ struct bmfp_solver_s
   void *work_b = nullptr;
   void *work_c = nullptr;               // best iterate kept across restarts
   void *work_d = nullptr;               // best iterate within one run (WideEngine::run snapshot)
+  bool fp32_stalls = false;             // MIXED: an earlier solve had to finish in FP64
 
   ~bmfp_solver_s ()
   {
@@ -157,6 +158,16 @@ int solve_mixed (bmfp_solver_s *sv, const void *d_b, bmfp_solve_info *info, cuda
   void *r64 = sv->work_a; // FP64 residual
   void *r32 = sv->work_b; // scaled FP32 right-hand side of the inner solve
   BMFP_CUDA (cudaMemsetAsync (e64.x (), 0, sizeof (double) * (size_t) n, s));
+  if (sv->fp32_stalls && o.fallback_fp64)
+    {
+      // An earlier solve on this matrix found the FP32 inner solves unable to
+      // make progress (its conditioning is beyond FP32's reach, and it does
+      // not change between right-hand sides): go straight to FP64.
+      int rc = solve_plain (e64, d_b, r64, sv->work_c, sv->work_d, o, info, s);
+      info->used_fp64_fallback = 1;
+      info->iterations_fp32 = 0;
+      return rc;
+    }
   double prev_rel = INFINITY;
   int iters64 = 0, iters32 = 0;
   for (int k = 0;; k++)
@@ -184,6 +195,7 @@ int solve_mixed (bmfp_solver_s *sv, const void *d_b, bmfp_solve_info *info, cuda
             }
           // Finish in FP64 from the current x (restart from its true residual).
           info->used_fp64_fallback = 1;
+          sv->fp32_stalls = true;
           DevState st{};
           // A fresh count: this engine's device counter still holds the
           // last run of an earlier solve on the same solver.

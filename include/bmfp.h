@@ -335,9 +335,10 @@ BMFP_API int bmfp_batch_destroy (bmfp_batch_t b);
  * Continuous batching of solve requests on one GPU (no counterpart in the
  * reference). Requests (a resident FP64 matrix handle and a host right-hand
  * side) are admitted in arrival order while their device memory fits the HBM
- * budget and the in-flight limit, and what was admitted is launched at once
- * as a micro-batch of the batched kernel on one of several streams, so new
- * requests start while earlier ones are still on the GPU. Requests with more
+ * budget and the in-flight limit, and launched as a micro-batch of the
+ * batched kernel on an idle stream, so new requests start while earlier ones
+ * are still on the GPU; while every stream is busy, arrivals wait and the next
+ * launch takes up to max_batch of them at once. Requests with more
  * than wide_threshold_rows rows run on whole-GPU engine lanes. Matrices stay
  * resident (the caller keeps the handles alive until the server is
  * destroyed); each request's Krylov state lives on the device from admission
@@ -350,9 +351,9 @@ typedef struct bmfp_server_options
   size_t hbm_budget_bytes;     /* device bytes for admitted requests (default 120 GiB) */
   int max_in_flight;           /* requests on the device at once (default 4096) */
   int max_batch;               /* requests per micro-batch launch (default 64) */
-  int streams;                 /* micro-batch streams (default 48) */
+  int streams;                 /* concurrent micro-batches (default 8) */
   int cluster_size;            /* CTAs per system team (default 4) */
-  int threads_per_cta;         /* default 256 */
+  int threads_per_cta;         /* default 512 */
   int64_t wide_threshold_rows; /* larger requests use the whole-GPU engine (default 200000) */
   int wide_lanes;              /* whole-GPU solves run concurrently (default 4) */
   bmfp_solver_options solver;  /* precision, tolerance, limits; no preconditioner */
