@@ -10,6 +10,7 @@ Python or CPU fallback.
 from __future__ import annotations
 
 import ctypes
+import os
 
 import numpy as np
 
@@ -167,6 +168,21 @@ def csr_to_bcsr(row_ptr, cols, vals, n_cols, bs):
     check(L.bmfp_csr_to_bcsr(e, n_rows, n_cols, bs, _p(row_ptr), _p(cols), _p(vals), _p(brp),
                              ctypes.byref(nnzb), _p(bc), _p(bv)))
     return brp, bc, bv
+
+
+def mm_read_csr(path, dtype=np.float64):
+    """MatrixMarket coordinate file -> (row_ptr, cols, vals, n_cols) through
+    bmfp_mm_read_csr; bs-blocked with csr_to_bcsr(row_ptr, cols, vals, n_cols, bs)."""
+    m, n, nnz = ctypes.c_int(), ctypes.c_int(), ctypes.c_int64()
+    e = dtype_enum(dtype)
+    p = os.fsencode(path)
+    check(load().bmfp_mm_read_csr(p, e, ctypes.byref(m), ctypes.byref(n), ctypes.byref(nnz), None, None, None))
+    rp = np.empty(m.value + 1, np.int32)
+    cols = np.empty(nnz.value, np.int32)
+    vals = np.empty(nnz.value, np_dtype(e))
+    check(load().bmfp_mm_read_csr(p, e, ctypes.byref(m), ctypes.byref(n), ctypes.byref(nnz), _p(rp), _p(cols),
+                                  _p(vals)))
+    return rp, cols, vals, n.value
 
 
 def transpose_blocks(row_ptr, vals, bs):

@@ -12,8 +12,12 @@
 #include "internal.h"
 
 #include <algorithm>
+#include <cctype>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 
 namespace bmfp
@@ -472,3 +476,194 @@ int bmfp_gen_q4_elasticity (int dtype, int nx, int ny, double young, double pois
 }
 
 } // extern "C"
+
+// ------------------------------------------------------------ MatrixMarket
+
+namespace
+{
+struct MmEntry
+{
+  int row, col;
+  int64_t order; // position in the file, to sum duplicates in file order
+  double value;
+};
+
+struct MmFile
+{
+  int n_rows = 0, n_cols = 0;
+  std::vector<MmEntry> entries;
+};
+
+std::string lower (std::string t)
+{
+  for (char &ch : t)
+    ch = (char) std::tolower ((unsigned char) ch);
+  return t;
+}
+
+// Reads the whole file: banner, comments, size line, entries (1-based).
+int mm_parse (const char *path, MmFile &out)
+{
+  FILE *f = std::fopen (path, "r");
+  if (!f)
+    return fail (BMFP_ERROR_INVALID_VALUE, "cannot open %s", path);
+  struct Closer
+  {
+    FILE *f;
+    ~Closer () { std::fclose (f); }
+  } closer{ f };
+  char line[4096];
+  if (!std::fgets (line, sizeof line, f))
+    return fail (BMFP_ERROR_INVALID_VALUE, "%s: empty file", path);
+  char w[5][64] = {};
+  if (std::sscanf (line, "%63s %63s %63s %63s %63s", w[0], w[1], w[2], w[3], w[4]) != 5
+      || lower (w[0]) != "%%matrixmarket" || lower (w[1]) != "matrix")
+    return fail (BMFP_ERROR_INVALID_VALUE, "%s: not a MatrixMarket matrix banner", path);
+  const std::string format = lower (w[2]), field = lower (w[3]), symmetry = lower (w[4]);
+  if (format != "coordinate")
+    return fail (BMFP_ERROR_NOT_SUPPORTED, "%s: only coordinate (sparse) files are read", path);
+  const bool pattern = field == "pattern";
+  if (!pattern && field != "real" && field != "double" && field != "integer")
+    return fail (BMFP_ERROR_NOT_SUPPORTED, "%s: field '%s' is not read", path, field.c_str ());
+  int mirror = 0; // 0 general, 1 symmetric, -1 skew-symmetric
+  if (symmetry == "symmetric")
+    mirror = 1;
+  else if (symmetry == "skew-symmetric")
+    mirror = -1;
+  else if (symmetry != "general")
+    return fail (BMFP_ERROR_NOT_SUPPORTED, "%s: symmetry '%s' is not read", path, symmetry.c_str ());
+  long long m = -1, n = -1, nz = -1;
+  while (std::fgets (line, sizeof line, f))
+    {
+      if (line[0] == '%')
+        continue;
+      if (std::sscanf (line, "%lld %lld %lld", &m, &n, &nz) == 3)
+        break;
+      bool blank = true;
+      for (const char *c = line; *c; c++)
+        blank = blank && std::isspace ((unsigned char) *c);
+      if (!blank)
+        return fail (BMFP_ERROR_INVALID_VALUE, "%s: bad size line", path);
+    }
+  if (m < 0 || n < 0 || nz < 0 || m > INT32_MAX || n > INT32_MAX)
+    return fail (BMFP_ERROR_INVALID_VALUE, "%s: bad or missing size line", path);
+  if ((mirror != 0) && m != n)
+    return fail (BMFP_ERROR_INVALID_VALUE, "%s: symmetric file of a non-square matrix", path);
+  out.n_rows = (int) m;
+  out.n_cols = (int) n;
+  out.entries.clear ();
+  out.entries.reserve ((size_t) nz * (mirror ? 2 : 1));
+  int64_t k = 0;
+  while (k < nz && std::fgets (line, sizeof line, f))
+    {
+      if (line[0] == '%')
+        continue;
+      char *p = line, *end = nullptr;
+      const long long i = std::strtoll (p, &end, 10);
+      if (end == p)
+        {
+          bool blank = true;
+          for (const char *c = line; *c; c++)
+            blank = blank && std::isspace ((unsigned char) *c);
+          if (blank)
+            continue;
+          return fail (BMFP_ERROR_INVALID_VALUE, "%s: bad entry %lld", path, (long long) k + 1);
+        }
+      p = end;
+      const long long j = std::strtoll (p, &end, 10);
+      if (end == p)
+        return fail (BMFP_ERROR_INVALID_VALUE, "%s: bad entry %lld", path, (long long) k + 1);
+      p = end;
+      double v = 1.0;
+      if (!pattern)
+        {
+          v = std::strtod (p, &end);
+          if (end == p)
+            return fail (BMFP_ERROR_INVALID_VALUE, "%s: entry %lld has no value", path, (long long) k + 1);
+        }
+      if (i < 1 || i > m || j < 1 || j > n)
+        return fail (BMFP_ERROR_INVALID_VALUE, "%s: entry %lld (%lld, %lld) outside %lld x %lld", path,
+                     (long long) k + 1, i, j, m, n);
+      out.entries.push_back ({ (int) (i - 1), (int) (j - 1), 2 * k, v });
+      if (mirror && i != j)
+        out.entries.push_back ({ (int) (j - 1), (int) (i - 1), 2 * k + 1, mirror * v });
+      k++;
+    }
+  if (k != nz)
+    return fail (BMFP_ERROR_INVALID_VALUE, "%s: %lld of %lld entries present", path, (long long) k, nz);
+  // Rows ascending, columns ascending, duplicates kept in file order.
+  std::sort (out.entries.begin (), out.entries.end (), [] (const MmEntry &a, const MmEntry &b) {
+    if (a.row != b.row)
+      return a.row < b.row;
+    if (a.col != b.col)
+      return a.col < b.col;
+    return a.order < b.order;
+  });
+  return BMFP_SUCCESS;
+}
+
+template <typename T> void mm_fill (const MmFile &mf, int *rp, int *cols, T *vals)
+{
+  std::fill (rp, rp + mf.n_rows + 1, 0);
+  int64_t e = -1;
+  int prev_row = -1, prev_col = -1;
+  double acc = 0.0;
+  auto flush = [&] () {
+    if (e >= 0)
+      vals[e] = (T) acc;
+  };
+  for (const MmEntry &m : mf.entries)
+    {
+      if (m.row == prev_row && m.col == prev_col)
+        {
+          acc += m.value;
+          continue;
+        }
+      flush ();
+      e++;
+      cols[e] = m.col;
+      rp[m.row + 1]++;
+      acc = m.value;
+      prev_row = m.row;
+      prev_col = m.col;
+    }
+  flush ();
+  for (int r = 0; r < mf.n_rows; r++)
+    rp[r + 1] += rp[r];
+}
+
+int64_t mm_distinct (const MmFile &mf)
+{
+  int64_t nnz = 0;
+  for (size_t k = 0; k < mf.entries.size (); k++)
+    if (k == 0 || mf.entries[k].row != mf.entries[k - 1].row || mf.entries[k].col != mf.entries[k - 1].col)
+      nnz++;
+  return nnz;
+}
+} // namespace
+
+int bmfp_mm_read_csr (const char *path, int dtype, int *n_rows, int *n_cols, int64_t *nnz, int *row_ptr,
+                      int *cols, void *values)
+{
+  if (!path || !dtype_ok (dtype) || !n_rows || !n_cols || !nnz)
+    return fail (BMFP_ERROR_INVALID_VALUE, "invalid arguments");
+  MmFile mf;
+  int st = mm_parse (path, mf);
+  if (st != BMFP_SUCCESS)
+    return st;
+  const int64_t distinct = mm_distinct (mf);
+  if (distinct > INT32_MAX)
+    return fail (BMFP_ERROR_NOT_SUPPORTED, "more than 2^31-1 entries");
+  *n_rows = mf.n_rows;
+  *n_cols = mf.n_cols;
+  *nnz = distinct;
+  if (!row_ptr)
+    return BMFP_SUCCESS;
+  if (distinct > 0 && (!cols || !values))
+    return fail (BMFP_ERROR_INVALID_VALUE, "null output array");
+  if (dtype == BMFP_R64F)
+    mm_fill (mf, row_ptr, cols, (double *) values);
+  else
+    mm_fill (mf, row_ptr, cols, (float *) values);
+  return BMFP_SUCCESS;
+}

@@ -450,6 +450,17 @@ BMFP_API int bmfp_gen_uniform_vector (int dtype, int64_t n, uint64_t seed, uint6
 BMFP_API int bmfp_gen_q4_elasticity (int dtype, int nx, int ny, double young, double poisson,
                                      int *row_ptr, int64_t *nnzb, int *cols, void *vals,
                                      void *rhs);
+/* MatrixMarket coordinate file -> CSR (new; the reference only writes such
+ * files, csr_matrix_class::write_mm, common/matrix_converters.h:119-144, with
+ * common/mmio.c). Fields real, double, integer or pattern (1.0); symmetry
+ * general, symmetric or skew-symmetric (the other triangle mirrored);
+ * entries in any order, duplicates summed in file order; output rows
+ * ascending, columns ascending within a row. Values are parsed as double and
+ * rounded once to dtype. Pass 1 (row_ptr == NULL): *n_rows, *n_cols, *nnz.
+ * Pass 2: row_ptr (n_rows+1), cols and values (nnz). Together with
+ * bmfp_csr_to_bcsr this brings any MatrixMarket matrix to the kernels. */
+BMFP_API int bmfp_mm_read_csr (const char *path, int dtype, int *n_rows, int *n_cols, int64_t *nnz,
+                               int *row_ptr, int *cols, void *values);
 /* Algorithmic bytes of one BCSR SpMV: values + block columns + row offsets +
  * x read once + y written once (value and vector size from dtype). */
 BMFP_API int64_t bmfp_bcsr_spmv_bytes (int dtype, int n_block_rows, int n_block_cols, int bs,
