@@ -89,6 +89,8 @@ def parse_args():
                                                                           "takes a whole-GPU lane")
     ap.add_argument("--no-baseline", action="store_true", help="serve: skip the FIFO per-request baseline")
     ap.add_argument("--large-fraction", type=float, default=0.05, help="serve: share of 1000x250 requests")
+    ap.add_argument("--cluster-size", type=int, default=None, help="serve: CTAs per system team")
+    ap.add_argument("--threads-per-cta", type=int, default=None, help="serve: threads per team CTA")
     ap.add_argument("--grid", default="200x50", help="solve: nodes nx x ny of the Q4 grid")
     ap.add_argument("--precision", default="fp64", choices=("fp64", "fp32", "mixed", "both"))
     ap.add_argument("--tol", type=float, default=1e-10)
@@ -651,6 +653,10 @@ def run_serve(args):
         kw["wide_lanes"] = args.wide_lanes
     if args.wide_threshold is not None:
         kw["wide_threshold_rows"] = args.wide_threshold
+    if args.cluster_size is not None:
+        kw["cluster_size"] = args.cluster_size
+    if args.threads_per_cta is not None:
+        kw["threads_per_cta"] = args.threads_per_cta
     srv = bm.Server(args.precision, tol=args.tol, max_iters=args.max_iters, **kw)
     # warm-up: one small request
     w = np.zeros(mats[min(mats)].rows)

@@ -541,6 +541,13 @@ __device__ void solve_system (cg::cluster_group &cl, const BatchDesc &D, const B
           cl.sync ();
         }
     }
+  if (D.x_out)
+    {
+      for (int64_t i = ix.elem0; i < D.n; i += ix.elem_stride)
+        D.x_out[i] = D.x[i];
+      __threadfence_system ();
+      cl.sync (); // every team thread's part of x is out before done is set
+    }
   if (cl.block_rank () == 0 && threadIdx.x == 0)
     {
       // Converged means the FP64 true residual met the tolerance; a solve
@@ -554,6 +561,8 @@ __device__ void solve_system (cg::cluster_group &cl, const BatchDesc &D, const B
       res.fallback = fallback;
       res.true_rel = rel;
       res.rec_rel = rec;
+      __threadfence_system ();
+      *reinterpret_cast<volatile int *> (&res.done) = 1;
     }
 }
 

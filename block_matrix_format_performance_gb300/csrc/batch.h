@@ -19,13 +19,19 @@ struct BatchDesc
   double *x = nullptr;
   double *w64 = nullptr; // 9 n: r, rh, p, v, s, t, residual, best x, in-run snapshot
   float *w32 = nullptr;  // 8 n: r, rh, p, v, s, t, x32, rhs32
+  double *x_out = nullptr; // optional copy of x as each system finishes (mapped host memory)
 };
 
+// Result of one system. With `out` in mapped host memory (the serving loop),
+// `done` is written last, after a system-scope fence, so the host can take a
+// finished system while the rest of its launch still runs.
 struct BatchOut
 {
   int status = 0; // 1 converged, 2 limit, 3 breakdown
   int iterations = 0, iterations_fp32 = 0, refinements = 0, restarts = 0, fallback = 0;
   double true_rel = 0.0, rec_rel = 0.0;
+  int done = 0;
+  int pad = 0;
 };
 
 struct BatchParams

@@ -66,6 +66,8 @@ struct MicroBatch
   BatchDesc *h_desc = nullptr;
   BatchOut *h_out = nullptr;
   std::vector<double *> h_x; // pinned copies of each request's x
+  std::vector<char> taken;   // request already handed back
+  size_t req_bytes = 0;      // budget bytes of all its requests, released at the end
   cudaEvent_t done = nullptr;
 };
 
@@ -93,11 +95,17 @@ public:
     while (c < bytes)
       c <<= 1;
     void *p = nullptr;
-    if (cudaMallocHost (&p, c) != cudaSuccess)
+    if (cudaHostAlloc (&p, c, cudaHostAllocMapped) != cudaSuccess)
       return nullptr;
     all_.push_back (p);
     *cap = c;
     return (char *) p;
+  }
+  // Device address of page-locked memory the kernels write to directly.
+  static char *device_alias (char *h)
+  {
+    void *d = nullptr;
+    return cudaHostGetDevicePointer (&d, h, 0) == cudaSuccess ? (char *) d : nullptr;
   }
   void give (char *p, size_t cap)
   {
@@ -192,13 +200,19 @@ int launch_micro_batch (bmfp_server_s *sv, std::vector<Request *> &reqs, int str
   mb->stream = stream;
   cudaStream_t s = sv->streams[mb->stream];
   const int n = (int) reqs.size ();
-  size_t total = align256 (sizeof (BatchDesc) * n) + align256 (sizeof (BatchOut) * n) + 256 + align256 (sizeof (int) * n);
+  size_t total = align256 (sizeof (BatchDesc) * n) + 256 + align256 (sizeof (int) * n);
   for (Request *r : reqs)
-    total += r->bytes;
+    {
+      total += r->bytes;
+      mb->req_bytes += r->bytes;
+    }
+  mb->taken.assign (n, 0);
   BMFP_CUDA (cudaMallocFromPoolAsync (&mb->d_mem, total, sv->pool, s));
   mb->bytes = total;
-  // Pinned staging: descriptors, results, launch order, then b and x of
-  // every request (x comes back here and is copied out on retirement).
+  // Pinned, mapped staging: descriptors, results, launch order, then b and x
+  // of every request. The kernel writes each system's result and x here as
+  // soon as it finishes, so a request leaves without waiting for the slowest
+  // system of its launch.
   size_t hbytes = align256 (sizeof (BatchDesc) * n) + align256 (sizeof (BatchOut) * n) + align256 (sizeof (int) * n);
   for (Request *r : reqs)
     hbytes += 2 * align256 (sizeof (double) * r->n);
@@ -208,6 +222,14 @@ int launch_micro_batch (bmfp_server_s *sv, std::vector<Request *> &reqs, int str
       cudaFreeAsync (mb->d_mem, s);
       return fail (BMFP_ERROR_OUT_OF_MEMORY, "page-locked staging of %zu bytes failed", hbytes);
     }
+  char *dev_slab = PinnedPool::device_alias (mb->h_slab);
+  if (!dev_slab)
+    {
+      sv->pinned.give (mb->h_slab, mb->h_cap);
+      cudaFreeAsync (mb->d_mem, s);
+      return fail (BMFP_ERROR_CUDA, "page-locked staging is not mapped into the device");
+    }
+  auto dev_of = [&] (const void *h) { return dev_slab + ((const char *) h - mb->h_slab); };
   char *hp = mb->h_slab;
   mb->h_desc = (BatchDesc *) hp;
   hp += align256 (sizeof (BatchDesc) * n);
@@ -219,8 +241,8 @@ int launch_micro_batch (bmfp_server_s *sv, std::vector<Request *> &reqs, int str
   char *p = (char *) mb->d_mem;
   BatchDesc *d_desc = (BatchDesc *) p;
   p += align256 (sizeof (BatchDesc) * n);
-  BatchOut *d_out = (BatchOut *) p;
-  p += align256 (sizeof (BatchOut) * n);
+  std::memset ((void *) mb->h_out, 0, sizeof (BatchOut) * n);
+  BatchOut *d_out = (BatchOut *) dev_of (mb->h_out);
   int *d_counter = (int *) p;
   p += 256;
   int *d_order = (int *) p;
@@ -260,6 +282,7 @@ int launch_micro_batch (bmfp_server_s *sv, std::vector<Request *> &reqs, int str
       D.x = r->d_x;
       D.w64 = r->w64;
       D.w32 = r->w32;
+      D.x_out = r->h_x ? (double *) dev_of (mb->h_x[i]) : nullptr;
       order[i] = i;
     }
   std::stable_sort (order.begin (), order.end (), [&] (int a, int b) { return reqs[a]->n > reqs[b]->n; });
@@ -286,10 +309,6 @@ int launch_micro_batch (bmfp_server_s *sv, std::vector<Request *> &reqs, int str
                          clusters * sv->opts.cluster_size, s);
   if (rc != BMFP_SUCCESS)
     return rc;
-  BMFP_CUDA (cudaMemcpyAsync (mb->h_out, d_out, sizeof (BatchOut) * n, cudaMemcpyDeviceToHost, s));
-  for (int i = 0; i < n; i++)
-    if (reqs[i]->h_x)
-      BMFP_CUDA (cudaMemcpyAsync (mb->h_x[i], reqs[i]->d_x, sizeof (double) * reqs[i]->n, cudaMemcpyDeviceToHost, s));
   BMFP_CUDA (cudaEventCreateWithFlags (&mb->done, cudaEventDisableTiming));
   BMFP_CUDA (cudaEventRecord (mb->done, s));
   for (Request *r : reqs)
@@ -300,13 +319,43 @@ int launch_micro_batch (bmfp_server_s *sv, std::vector<Request *> &reqs, int str
   return BMFP_SUCCESS;
 }
 
-// Retire completed micro-batches (lock held). Returns true if any finished.
+// Hand back one request of a micro-batch (lock held). After finish() the
+// waiter may free the Request at any moment, so the slot is cleared.
+void take_request (bmfp_server_s *sv, MicroBatch *mb, size_t i, bool ok)
+{
+  Request *r = mb->reqs[i];
+  const BatchOut &o = mb->h_out[i];
+  if (ok && r->h_x)
+    std::memcpy (r->h_x, mb->h_x[i], sizeof (double) * r->n);
+  bmfp_solve_info &f = r->info;
+  f.status = !ok ? BMFP_ERROR_CUDA
+                 : (o.status == 1 ? BMFP_SUCCESS : (o.status == 3 ? BMFP_ERROR_BREAKDOWN : BMFP_ERROR_NOT_CONVERGED));
+  f.iterations = o.iterations;
+  f.iterations_fp32 = o.iterations_fp32;
+  f.refinements = o.refinements;
+  f.restarts = o.restarts;
+  f.used_fp64_fallback = o.fallback;
+  f.true_rel_residual = o.true_rel;
+  f.recursive_rel_residual = o.rec_rel;
+  mb->taken[i] = 1;
+  mb->reqs[i] = nullptr;
+  finish (sv, r);
+}
+
+// Hand back the requests whose systems have finished, and retire completed
+// micro-batches (lock held). Returns true if any request finished.
 bool retire (bmfp_server_s *sv)
 {
   bool any = false;
   for (size_t k = 0; k < sv->running.size ();)
     {
       MicroBatch *mb = sv->running[k].get ();
+      for (size_t i = 0; i < mb->reqs.size (); i++)
+        if (!mb->taken[i] && *reinterpret_cast<volatile int *> (&mb->h_out[i].done))
+          {
+            take_request (sv, mb, i, true);
+            any = true;
+          }
       const cudaError_t q = cudaEventQuery (mb->done);
       if (q == cudaErrorNotReady)
         {
@@ -316,26 +365,13 @@ bool retire (bmfp_server_s *sv)
       if (q != cudaSuccess && sv->error == BMFP_SUCCESS)
         sv->error = cuda_fail (q, "micro-batch", __FILE__, __LINE__);
       for (size_t i = 0; i < mb->reqs.size (); i++)
-        {
-          Request *r = mb->reqs[i];
-          const BatchOut &o = mb->h_out[i];
-          if (q == cudaSuccess && r->h_x)
-            std::memcpy (r->h_x, mb->h_x[i], sizeof (double) * r->n);
-          bmfp_solve_info &f = r->info;
-          f.status = q != cudaSuccess ? BMFP_ERROR_CUDA
-                                      : (o.status == 1 ? BMFP_SUCCESS
-                                                       : (o.status == 3 ? BMFP_ERROR_BREAKDOWN : BMFP_ERROR_NOT_CONVERGED));
-          f.iterations = o.iterations;
-          f.iterations_fp32 = o.iterations_fp32;
-          f.refinements = o.refinements;
-          f.restarts = o.restarts;
-          f.used_fp64_fallback = o.fallback;
-          f.true_rel_residual = o.true_rel;
-          f.recursive_rel_residual = o.rec_rel;
-          sv->bytes_in_use -= r->bytes;
-          sv->in_flight--;
-          finish (sv, r);
-        }
+        if (!mb->taken[i])
+          {
+            take_request (sv, mb, i, q == cudaSuccess && mb->h_out[i].done);
+            any = true;
+          }
+      sv->bytes_in_use -= mb->req_bytes;
+      sv->in_flight -= (int) mb->reqs.size ();
       cudaFreeAsync (mb->d_mem, sv->streams[mb->stream]);
       sv->stream_busy[mb->stream] = 0;
       cudaEventDestroy (mb->done);

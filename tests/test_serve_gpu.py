@@ -67,7 +67,7 @@ def test_mix_equals_alone_bitwise(problems):
 
 def test_admission_respects_the_budget(problems):
     m, rp, c, v, _ = problems[4]  # 80x20 -> 3200 rows
-    per_request = 256 * 2 * ((m.rows * 8 + 255) // 256) + ((m.rows * 64 + 255) // 256) * 256
+    per_request = 256 * 2 * ((m.rows * 8 + 255) // 256) + ((m.rows * 72 + 255) // 256) * 256
     srv = bm.Server("fp64", tol=1e-10, hbm_budget_bytes=int(2.5 * per_request))
     xs = [np.zeros(m.rows) for _ in range(6)]
     bs = [loads(m.rows, k) for k in range(6)]
@@ -118,3 +118,41 @@ def test_mixed_precision_server(problems):
         info = srv.wait(t)
         assert info["status"] == bm.SUCCESS and rel_residual(rp, c, v, b, x) < 1e-10
     srv.close()
+
+
+def test_finished_request_leaves_before_its_micro_batch(problems):
+    """One stream: a first request occupies it, the next four wait and are
+    launched together (one slow 200x50 system, three 20x5). The small ones
+    come back while the slow one of the same launch is still running."""
+    rp, c, v, _ = bm.gen_q4_elasticity(200, 50)
+    big = bm.Matrix.from_bcsr(rp, c, v, 2)
+    srv = bm.Server("fp64", tol=1e-10, streams=1, max_batch=8)
+    first = srv.submit(big, loads(big.rows, 1), np.zeros(big.rows))
+    deadline = time.time() + 10
+    while srv.stats()["pending"] and time.time() < deadline:  # launched alone
+        time.sleep(1e-4)
+    b_slow = loads(big.rows, 2)
+    x_slow = np.zeros(big.rows)
+    slow = srv.submit(big, b_slow, x_slow)
+    small = []
+    for k in range(3):
+        m, rp0, c0, v0, _ = problems[0]
+        b = loads(m.rows, 10 + k)
+        x = np.zeros(m.rows)
+        small.append((rp0, c0, v0, b, x, srv.submit(m, b, x)))
+    srv.wait(first)
+    early, slow_info = 0, None
+    for rp0, c0, v0, b, x, t in small:
+        info = srv.wait(t)
+        assert info["status"] == bm.SUCCESS and rel_residual(rp0, c0, v0, b, x) < 1e-10
+        if slow_info is None:
+            slow_info = srv.poll(slow)
+            early += slow_info is None
+    if slow_info is None:
+        slow_info = srv.wait(slow)
+    assert slow_info["status"] == bm.SUCCESS and rel_residual(rp, c, v, b_slow, x_slow) < 1e-10
+    st = srv.stats()
+    srv.close()
+    big.close()
+    assert st["micro_batches"] == 2  # the first request, then the four together
+    assert early == 3
