@@ -382,6 +382,26 @@ bool retire (bmfp_server_s *sv)
   return any;
 }
 
+// Launch a micro-batch; if that fails, its requests end with the error (so
+// their waiters return and the server can still shut down) and the server
+// refuses further work.
+void launch_or_fail (bmfp_server_s *sv, std::vector<Request *> &reqs, int slot)
+{
+  const int rc = launch_micro_batch (sv, reqs, slot);
+  if (rc == BMFP_SUCCESS)
+    return;
+  if (sv->error == BMFP_SUCCESS)
+    sv->error = rc;
+  for (Request *r : reqs)
+    {
+      r->info.status = rc;
+      sv->bytes_in_use -= r->bytes;
+      sv->in_flight--;
+      finish (sv, r);
+    }
+  sv->cv_done.notify_all ();
+}
+
 void dispatcher_main (bmfp_server_s *sv)
 {
   cudaSetDevice (sv->device);
@@ -437,14 +457,13 @@ void dispatcher_main (bmfp_server_s *sv)
           admitted.push_back (r);
           if ((int) admitted.size () >= sv->opts.max_batch)
             {
-              if (launch_micro_batch (sv, admitted, slot) != BMFP_SUCCESS && sv->error == BMFP_SUCCESS)
-                sv->error = BMFP_ERROR_CUDA;
+              launch_or_fail (sv, admitted, slot);
               admitted.clear ();
               slot = free_stream ();
             }
         }
-      if (!admitted.empty () && launch_micro_batch (sv, admitted, slot) != BMFP_SUCCESS && sv->error == BMFP_SUCCESS)
-        sv->error = BMFP_ERROR_CUDA;
+      if (!admitted.empty ())
+        launch_or_fail (sv, admitted, slot);
       if (sv->stop && sv->pending.empty () && sv->running.empty () && sv->in_flight == 0)
         break;
       // Sleep until new work arrives or a short poll interval passes while
