@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import argparse
 import concurrent.futures as cf
+import fcntl
 import os
 import shutil
 import subprocess
@@ -87,10 +88,20 @@ def up_to_date() -> bool:
 
 
 def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -> str:
-    """Compile and link libbmfp.so; returns its path."""
+    """Compile and link libbmfp.so; returns its path. Processes that build at
+    the same time (one per rank under torchrun, parallel test workers) take
+    turns on a lock file; the later ones find the library up to date."""
     if not force and up_to_date():
         return LIB
     os.makedirs(BUILD, exist_ok=True)
+    with open(os.path.join(BUILD, ".lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        if not force and up_to_date():
+            return LIB
+        return _build_locked(verbose, jobs)
+
+
+def _build_locked(verbose: bool, jobs: int | None) -> str:
     srcs = _sources()
     objs = [os.path.join(BUILD, s.replace(".", "_") + ".o") for s in srcs]
     cmds = [_compile_cmd(s, o) for s, o in zip(srcs, objs)]
