@@ -92,6 +92,9 @@ def parse_args():
     ap.add_argument("--cluster-size", type=int, default=None, help="serve: CTAs per system team")
     ap.add_argument("--threads-per-cta", type=int, default=None, help="serve: threads per team CTA")
     ap.add_argument("--grid", default="200x50", help="solve: nodes nx x ny of the Q4 grid")
+    ap.add_argument("--matrix", default="q4", choices=("q4", "shifted"),
+                    help="solve: Q4 elasticity K (default) or the implicit-step operator K + shift * I")
+    ap.add_argument("--shift", type=float, default=1e-3, help="solve: shift of --matrix shifted")
     ap.add_argument("--precision", default="fp64", choices=("fp64", "fp32", "mixed", "both"))
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--max-iters", type=int, default=200000)
@@ -515,7 +518,10 @@ def run_solve(args):
     from block_matrix_format_performance_gb300 import build as B
     B.build()
     nx, ny = (int(t) for t in args.grid.lower().split("x"))
-    rp, c, v, rhs = bm.gen_q4_elasticity(nx, ny)
+    if args.matrix == "shifted":
+        rp, c, v, rhs = shifted_q4(nx, ny, args.shift)
+    else:
+        rp, c, v, rhs = bm.gen_q4_elasticity(nx, ny)
     A = bm.Matrix.from_bcsr(rp, c, v, 2)
     d_b = torch.from_numpy(rhs).cuda()
     n = 2 * nx * ny
@@ -534,7 +540,8 @@ def run_solve(args):
         out[prec] = {"solves_per_s": round(1.0 / best["seconds"], 3), "seconds": round(best["seconds"], 4),
                      "us_per_iteration": round(best["seconds"] / it * 1e6, 2), "bytes_per_iteration": int(per_iter),
                      "gbs_per_iteration": round(per_iter / (best["seconds"] / it) / 1e9, 1), **best}
-    line = {"workload": "solve", "grid": [nx, ny], "dofs": n, "nnzb": int(c.size), "tol": args.tol}
+    line = {"workload": "solve", "matrix": args.matrix if args.matrix == "q4" else f"q4+{args.shift:g}I",
+            "grid": [nx, ny], "dofs": n, "nnzb": int(c.size), "tol": args.tol}
     if len(out) == 1:
         line.update(precision=args.precision, **out[args.precision])
     else:
@@ -543,6 +550,20 @@ def run_solve(args):
         line["mixed_error_vs_fp64"] = float(torch.linalg.norm(xs["mixed"].double() - ref) / torch.linalg.norm(ref))
     print(json.dumps(line), flush=True)
     A.close()
+
+
+def shifted_q4(nx, ny, shift):
+    """The Q4 elasticity operator of an implicit time step, K + shift * I
+    (unit lumped mass, shift = 1 / dt^2): on the 200x50 grid shift 1e-3 gives
+    cond ~ 4e3 instead of K's 3e6, within reach of FP32 inner solves
+    (u32 * cond ~ 3e-4), so it shows what mixed precision buys on GB300 where
+    it can work."""
+    import block_matrix_format_performance_gb300 as bm
+    rp, c, v, rhs = bm.gen_q4_elasticity(nx, ny)
+    v = v.reshape(-1, 2, 2).copy()
+    rows = np.repeat(np.arange(nx * ny), np.diff(rp))
+    v[c == rows] += shift * np.eye(2)
+    return rp, c, v.reshape(-1), rhs
 
 
 def batch_grids(n_systems, seed=0):

@@ -174,21 +174,26 @@ template <typename T, int G> struct CsrOp
   }
 };
 
+// Dot-product accumulators of the SpMV epilogues and phase 5 run in T: each
+// thread sums a handful of terms, then warps, CTAs and the grid combine the
+// partials in FP64. For FP64 solves that is FP64 throughout; the FP32 engine
+// (inner solves of mixed precision, asked for 1e-4) keeps GB300's narrow
+// FP64 pipe out of its per-element work.
 template <typename T> struct EpiDot
 {
   const T *a;
-  double acc = 0.0;
-  __device__ void operator() (int64_t i, T y) { acc = fma ((double) a[i], (double) y, acc); }
+  T acc = 0;
+  __device__ void operator() (int64_t i, T y) { acc = fma (a[i], y, acc); }
 };
 
 template <typename T> struct EpiTS
 {
   const T *s;
-  double ts = 0.0, tt = 0.0;
+  T ts = 0, tt = 0;
   __device__ void operator() (int64_t i, T t)
   {
-    ts = fma ((double) s[i], (double) t, ts);
-    tt = fma ((double) t, (double) t, tt);
+    ts = fma (s[i], t, ts);
+    tt = fma (t, t, tt);
   }
 };
 
@@ -215,7 +220,7 @@ __global__ void __launch_bounds__ (kThreads) phase_v (Args<T> a)
     return;
   EpiDot<T> e{ a.rh };
   Op::run (a, a.q, a.v, e);
-  double vals[1] = { e.acc };
+  double vals[1] = { (double) e.acc };
   const int ks[1] = { kRhV };
   store_parts<1> (vals, a.part, a.grid, ks);
 }
@@ -228,7 +233,7 @@ __global__ void __launch_bounds__ (kThreads) phase_t (Args<T> a)
     return;
   EpiTS<T> e{ a.s };
   Op::run (a, a.z, a.t, e);
-  double vals[2] = { e.ts, e.tt };
+  double vals[2] = { (double) e.ts, (double) e.tt };
   const int ks[2] = { kTS, kTT };
   store_parts<2> (vals, a.part, a.grid, ks);
 }
@@ -472,7 +477,7 @@ __global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
   if (!isfinite (omega))
     return;
   const T ta = (T) sh_alpha, tw = (T) omega;
-  double rhr = 0.0, rr = 0.0;
+  T rhr = 0, rr = 0;
   const T *qa = PRE ? a.q : a.p;
   const T *za = PRE ? a.z : a.s;
   const int64_t stride = (int64_t) gridDim.x * blockDim.x;
@@ -499,8 +504,8 @@ __global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
           a.x[k] = xv[u] + ta * qv[u] + tw * zv[u]; // h = x + alpha q; x = h + omega z
           const T ri = sv[u] - tw * tv[u];           // :340-357
           a.r[k] = ri;
-          rhr = fma ((double) hv[u], (double) ri, rhr);
-          rr = fma ((double) ri, (double) ri, rr);
+          rhr = fma (hv[u], ri, rhr);
+          rr = fma (ri, ri, rr);
         }
     }
   for (; i < a.n; i += stride)
@@ -508,10 +513,10 @@ __global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
       a.x[i] = a.x[i] + ta * qa[i] + tw * za[i];
       const T ri = a.s[i] - tw * a.t[i];
       a.r[i] = ri;
-      rhr = fma ((double) a.rh[i], (double) ri, rhr);
-      rr = fma ((double) ri, (double) ri, rr);
+      rhr = fma (a.rh[i], ri, rhr);
+      rr = fma (ri, ri, rr);
     }
-  double vals[2] = { rhr, rr };
+  double vals[2] = { (double) rhr, (double) rr };
   const int kk[2] = { kRhR, kRR };
   store_parts<2> (vals, a.part, a.grid, kk);
   if (blockIdx.x == 0 && threadIdx.x == 0)
