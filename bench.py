@@ -573,7 +573,7 @@ def batch_grids(n_systems, seed=0):
     return [(int(nx), max(2, int(round(nx / 4)))) for nx in nxs]
 
 
-def measure_batch(precisions, tol, max_iters, repeats, n_systems=256, per_request=True, grid=None):
+def measure_batch(precisions, tol, max_iters, repeats, n_systems=256, per_request=True, grid=None, shift=None):
     """The uneven batch (nx log-uniform in [20, 400], ny = nx / 4, seeded): each
     precision solved by one persistent, graph-captured launch, and the plain
     FP64 per-request solver run system after system on the same GPU."""
@@ -583,7 +583,7 @@ def measure_batch(precisions, tol, max_iters, repeats, n_systems=256, per_reques
     grids = batch_grids(n_systems) if grid is None else [grid] * n_systems
     mats, rhs = [], []
     for nx, ny in grids:
-        rp, c, v, b = bm.gen_q4_elasticity(nx, ny)
+        rp, c, v, b = shifted_q4(nx, ny, shift) if shift else bm.gen_q4_elasticity(nx, ny)
         mats.append(bm.Matrix.from_bcsr(rp, c, v, 2))
         rhs.append(b)
     d_b = [torch.from_numpy(b).cuda() for b in rhs]
@@ -631,9 +631,11 @@ def run_batch(args):
     from block_matrix_format_performance_gb300 import build as B
     B.build()
     grid = tuple(int(t) for t in args.batch_grid.lower().split("x")) if args.batch_grid else None
+    shift = args.shift if args.matrix == "shifted" else None
     res = measure_batch([args.precision], args.tol, args.max_iters, args.repeats, args.systems,
-                        per_request=args.repeats > 0, grid=grid)
-    print(json.dumps({"workload": "batch", "precision": args.precision, **res}), flush=True)
+                        per_request=args.repeats > 0, grid=grid, shift=shift)
+    print(json.dumps({"workload": "batch", "precision": args.precision,
+                      "matrix": "q4" if shift is None else f"q4+{shift:g}I", **res}), flush=True)
 
 
 def serve_stream(n_requests, rate, seed=1, large_fraction=0.05):
@@ -660,7 +662,7 @@ def run_serve(args):
     arrivals, grids = serve_stream(args.requests, args.rate, large_fraction=args.large_fraction)
     mats = {}
     for g in sorted(set(grids)):
-        rp, c, v, _ = bm.gen_q4_elasticity(*g)
+        rp, c, v, _ = shifted_q4(*g, args.shift) if args.matrix == "shifted" else bm.gen_q4_elasticity(*g)
         mats[g] = bm.Matrix.from_bcsr(rp, c, v, 2)
     rng = np.random.default_rng(7)
     rhs = []
@@ -735,7 +737,8 @@ def run_serve(args):
     bad = [{"grid": list(grids[k]), "status": i["status"], "true_rel": i["true_rel_residual"]}
            for k, i in enumerate(infos) if i["status"] != 0][:12]
     print(json.dumps({
-        "workload": "serve", "requests": len(grids), "rate_req_s": args.rate, "precision": args.precision,
+        "workload": "serve", "matrix": "q4" if args.matrix == "q4" else f"q4+{args.shift:g}I",
+        "requests": len(grids), "rate_req_s": args.rate, "precision": args.precision,
         "tol": args.tol, "large_requests": int(sum(g == (1000, 250) for g in grids)),
         "makespan_s": round(makespan, 3), "solves_per_s": round(len(grids) / makespan, 2),
         "latency_p50_s": round(float(np.percentile(lat, 50)), 4), "latency_p99_s": round(float(np.percentile(lat, 99)), 4),
