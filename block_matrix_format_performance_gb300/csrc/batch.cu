@@ -706,7 +706,11 @@ int BatchEngine::init (int n, const bmfp_matrix_s *const *mats, const bmfp_solve
   for (int i = 0; i < n; i++)
     {
       const bmfp_matrix_s *A = mats[i];
+      // The page-locked array comes back uninitialised (or holding an
+      // earlier engine's bytes): start every descriptor from its defaults,
+      // so fields this engine does not use (x_out) are null.
       BatchDesc &D = h_desc_[i];
+      D = BatchDesc{};
       D.nbr = A->n_rows;
       D.bs = A->bs ? A->bs : 1;
       D.n = rows[i];

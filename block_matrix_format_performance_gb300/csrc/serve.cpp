@@ -269,6 +269,7 @@ int launch_micro_batch (bmfp_server_s *sv, std::vector<Request *> &reqs, int str
         }
       BMFP_CUDA (cudaMemcpyAsync (r->d_b, h_b, sizeof (double) * r->n, cudaMemcpyHostToDevice, s));
       BatchDesc &D = mb->h_desc[i];
+      D = BatchDesc{}; // recycled page-locked memory: start from the defaults
       const bmfp_matrix_s *A = r->A;
       D.nbr = A->n_rows;
       D.bs = A->bs ? A->bs : 1;
