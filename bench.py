@@ -65,9 +65,12 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-csr-compare", action="store_true")
+    ap.add_argument("--no-ref-variants", action="store_true",
+                    help="skip timing the reference's own kernels on the sweep matrices")
     ap.add_argument("--no-solver", action="store_true", help="skip the batched-solve part of the line")
     ap.add_argument("--no-autotune", action="store_true",
-                    help="use the built-in lane choices (the autotuner's GB300 picks) instead of timing candidates")
+                    help="use the autotuner's GB300 picks (built-in table, column owner at FP64 bs 16/32) "
+                         "instead of timing candidates")
     ap.add_argument("--sizes", default=",".join(map(str, BLOCK_SIZES)))
     ap.add_argument("--dtypes", default=",".join(DTYPES))
     ap.add_argument("--n-block-rows", type=int, default=NBR,
@@ -101,6 +104,10 @@ def parse_args():
     ap.add_argument("--repeats", type=int, default=3)
     ap.add_argument("--ctas-per-sm", type=int, default=0, help="solve: persistent grid of the solver (0 = default)")
     return ap.parse_args()
+
+
+# Sweep cases where bmfp_matrix_autotune picks BMFP_LANES_COL_OWNER on GB300.
+COLUMN_OWNER_CASES = {("f64", 16): 65, ("f64", 32): 65}
 
 
 def np_dt(tag):
@@ -261,7 +268,14 @@ def run_ours(args):
         cs["dx"] = torch.from_numpy(cs["x"]).cuda()
         cs["dy"] = torch.empty_like(cs["dx"])
         # the library's autotuner times every valid lane count on this matrix
-        cs["lanes"] = 0 if args.no_autotune else cs["m"].autotune(cs["dx"], cs["dy"])
+        if args.no_autotune:
+            # the autotuner's GB300 picks that the library's built-in table
+            # cannot make (the column owner needs the handle's column-major copy)
+            cs["lanes"] = COLUMN_OWNER_CASES.get((cs["tag"], cs["bs"]), 0)
+            if cs["lanes"]:
+                cs["m"].set_lanes(cs["lanes"])
+        else:
+            cs["lanes"] = cs["m"].autotune(cs["dx"], cs["dy"])
     flush_w = torch.empty(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB
     flush_r = torch.ones(128 << 20, dtype=torch.float32, device="cuda")  # 512 MB
 
@@ -353,6 +367,49 @@ def run_ours(args):
                 "native_speedup": round(ms / (per_case_ms[cases.index(cs)] / args.steps), 2)}
             del d_rp, d_c, d_v
 
+    # The reference's own kernels (restated one per format string, the same
+    # thread mappings) on the same matrices: row-major thread / warp per row,
+    # column-major thread per row (template), column-by-column (template) and
+    # cuSPARSE bsrmv. bs 1 is CSR, covered above.
+    ref_cmp = {}
+    if not args.no_ref_variants:
+        ref_variants = [bm.BCSR_ROW_THREAD, bm.BCSR_ROW_WARP, bm.BCSR_COL_THREAD_TEMPLATE,
+                        bm.BCSR_COL_BY_COL_TEMPLATE, bm.CUSPARSE_ROW]
+        for cs in cases:
+            if cs["bs"] == 1:
+                continue
+            d_rp, d_c, d_v = (torch.from_numpy(a).cuda() for a in (cs["rp"], cs["c"], cs["v"]))
+            d_vt = None
+            native_ms = per_case_ms[cases.index(cs)] / args.steps
+            res = {}
+            for var in ref_variants:
+                if bm.variant_layout(var) == 1 and d_vt is None:
+                    d_vt = torch.from_numpy(bm.transpose_blocks(cs["rp"], cs["v"], cs["bs"])).cuda()
+                vals = d_vt if bm.variant_layout(var) == 1 else d_v
+                try:
+                    bm.bcsr_spmv(var, d_rp, d_c, vals, cs["dx"], cs["dy"], cs["bs"])
+                except bm.BmfpError as e:
+                    if e.status == bm.ERROR_NOT_SUPPORTED:
+                        continue
+                    raise
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                reps, tot = 3, 0.0
+                for r in range(reps + 1):
+                    flush()
+                    e0.record(stream)
+                    bm.bcsr_spmv(var, d_rp, d_c, vals, cs["dx"], cs["dy"], cs["bs"])
+                    e1.record(stream)
+                    torch.cuda.synchronize()
+                    if r:
+                        tot += e0.elapsed_time(e1)
+                res[bm.variant_name(var)] = round(cs["bytes"] / (tot / reps * 1e-3) / 1e9, 1)
+            best = max(res, key=res.get)
+            ref_cmp[f"bs{cs['bs']}_{cs['tag']}"] = {
+                "best_reference_format": best, "best_reference_gbs": res[best],
+                "native_speedup": round(cs["bytes"] / (native_ms * 1e-3) / 1e9 / res[best], 2), "gbs": res}
+            del d_rp, d_c, d_v, d_vt
+            torch.cuda.empty_cache()
+
     # End to end through the C ABI with host buffers: bmfp_bcsr_spmv_host
     # takes the pinned host arrays, uploads them in chunks overlapped with the
     # product and returns y in host memory, so every step moves the whole
@@ -408,6 +465,7 @@ def run_ours(args):
             "block_sizes": sizes, "seed": SEED, "parallelism": f"replicas x{world} (no collective)",
             "l2": "flushed before every product (256 MB write + 512 MB read), outside the timed events",
             "kernel": "GPU BCSR (GB300 native)", "per_case": per_case, "csr_warp_per_row": csr_cmp,
+            "reference_variants": ref_cmp,
             "wall_s_timed_region": round(wall, 3), "generate_s": round(gen_s, 1),
         },
         "roofline": {"bound": "hbm", "kernel": dom_key, "achieved": round(achieved, 1), "peak": hbm,

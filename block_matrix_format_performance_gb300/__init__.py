@@ -27,6 +27,7 @@ BCSR_COL_COAL_X, BCSR_COL_COAL_X_TEMPLATE = 7, 8
 BCSR_COL_BY_COL, BCSR_COL_BY_COL_FASTDIV, BCSR_COL_BY_COL_PO2, BCSR_COL_BY_COL_TEMPLATE = 9, 10, 11, 12
 BCSR_JIT, CUSPARSE_ROW, CUSPARSE_COL, BCSR_NATIVE = 13, 14, 15, 16
 VARIANT_COUNT = 17
+LANES_ROW_OWNER, LANES_COL_OWNER = 64, 65
 
 SUCCESS, ERROR_INVALID_VALUE, ERROR_CUDA, ERROR_OUT_OF_MEMORY, ERROR_NOT_SUPPORTED = 0, 1, 2, 3, 4
 ERROR_BREAKDOWN, ERROR_NOT_CONVERGED, ERROR_TIMEOUT, ERROR_BUDGET, PENDING = 5, 6, 7, 8, 9
@@ -309,6 +310,10 @@ class Matrix:
     def spmv(self, x, y, stream=None):
         check(load().bmfp_matrix_spmv(self.handle, _p(x), _p(y), _stream(stream)))
         return y
+
+    def set_lanes(self, lanes, stream=None):
+        """Pin the mapping (LANES_COL_OWNER builds the column-major copy)."""
+        check(load().bmfp_matrix_set_lanes(self.handle, lanes, _stream(stream)))
 
     def autotune(self, x, y, stream=None) -> int:
         g = ctypes.c_int(0)

@@ -218,6 +218,7 @@ static void matrix_free (bmfp_matrix_s *m)
   cudaFree (m->d_row_ptr);
   cudaFree (m->d_cols);
   cudaFree (m->d_vals);
+  cudaFree (m->d_vals_cm);
   delete m;
 }
 
@@ -388,15 +389,66 @@ int bmfp_matrix_device_arrays (bmfp_matrix_t m, const int **d_row_ptr, const int
   return BMFP_SUCCESS;
 }
 
+static bool col_owner_bs (int bs) { return bs == 4 || bs == 8 || bs == 16 || bs == 32; }
+
+// Builds (or, for any other mapping, releases) the column-major copy the
+// column-owner kernel reads.
+static int matrix_apply_lanes (bmfp_matrix_s *m, int lanes, cudaStream_t s)
+{
+  if (lanes == BMFP_LANES_COL_OWNER)
+    {
+      if (m->bs == 0 || !col_owner_bs (m->bs))
+        return fail (BMFP_ERROR_INVALID_VALUE, "column-owner mapping needs a BCSR handle with bs in {4,8,16,32}");
+      if (!m->d_vals_cm)
+        {
+          const size_t bytes = dtype_size (m->dtype) * (size_t) std::max<int64_t> (m->nnz * m->bs * m->bs, 1);
+          void *p = nullptr;
+          const cudaError_t e = cudaMalloc (&p, bytes);
+          if (e != cudaSuccess)
+            {
+              cudaGetLastError ();
+              return fail (BMFP_ERROR_OUT_OF_MEMORY, "no room for the column-major copy (%zu bytes)", bytes);
+            }
+          const int st = transpose_blocks_device (m->dtype, m->nnz, m->bs, m->d_vals, p, s);
+          if (st != BMFP_SUCCESS)
+            {
+              cudaFree (p);
+              return st;
+            }
+          m->d_vals_cm = p;
+        }
+    }
+  else if (m->d_vals_cm)
+    {
+      BMFP_CUDA (cudaStreamSynchronize (s)); // no product may still read it
+      cudaFree (m->d_vals_cm);
+      m->d_vals_cm = nullptr;
+    }
+  m->lanes = lanes;
+  return BMFP_SUCCESS;
+}
+
+int bmfp_matrix_set_lanes (bmfp_matrix_t m, int lanes, void *stream)
+{
+  if (!m)
+    return fail (BMFP_ERROR_INVALID_VALUE, "null matrix");
+  if (lanes < 0 || (lanes > 32 && lanes != BMFP_LANES_ROW_OWNER && lanes != BMFP_LANES_COL_OWNER))
+    return fail (BMFP_ERROR_INVALID_VALUE, "invalid lane count %d", lanes);
+  return matrix_apply_lanes (m, lanes, as_stream (stream));
+}
+
 int bmfp_matrix_spmv (bmfp_matrix_t m, const void *d_x, void *d_y, void *stream)
 {
   if (!m || !d_x || !d_y)
     return fail (BMFP_ERROR_INVALID_VALUE, "null argument");
+  if (m->lanes == BMFP_LANES_COL_OWNER && m->d_vals_cm)
+    return spmv_native_bcsr_colmajor (m->dtype, m->n_rows, m->bs, m->d_row_ptr, m->d_cols, m->d_vals_cm, d_x,
+                                      d_y, as_stream (stream));
   if (m->bs == 0)
     return spmv_native_csr (m->dtype, m->n_rows, m->nnz, m->d_row_ptr, m->d_cols, m->d_vals, d_x,
                             d_y, m->lanes, as_stream (stream));
-  return spmv_native_bcsr (m->dtype, m->n_rows, m->bs, m->nnz, m->d_row_ptr, m->d_cols,
-                           m->d_vals, d_x, d_y, m->lanes, as_stream (stream));
+  return spmv_native_bcsr (m->dtype, m->n_rows, m->bs, m->nnz, m->d_row_ptr, m->d_cols, m->d_vals, d_x, d_y,
+                           m->lanes == BMFP_LANES_COL_OWNER ? 0 : m->lanes, as_stream (stream));
 }
 
 int bmfp_matrix_autotune (bmfp_matrix_t m, const void *d_x, void *d_y, void *stream,
@@ -404,9 +456,11 @@ int bmfp_matrix_autotune (bmfp_matrix_t m, const void *d_x, void *d_y, void *str
 {
   if (!m || !d_x || !d_y)
     return fail (BMFP_ERROR_INVALID_VALUE, "null argument");
-  int cand[10];
+  int cand[12];
   const int bs_eff = m->bs ? m->bs : 1;
   int nc = native_lane_candidates (m->dtype, bs_eff, cand, 10);
+  if (m->bs && col_owner_bs (m->bs))
+    cand[nc++] = BMFP_LANES_COL_OWNER;
   if (nc == 0)
     {
       if (chosen_lanes)
@@ -414,6 +468,23 @@ int bmfp_matrix_autotune (bmfp_matrix_t m, const void *d_x, void *d_y, void *str
       return BMFP_SUCCESS;
     }
   cudaStream_t s = as_stream (stream);
+  // Each timed product starts with L2 emptied (a read of twice its size),
+  // as in repeated products over matrices that do not stay in L2: products
+  // back to back would favour whatever mapping the leftovers suit.
+  int dev = 0, l2 = 0;
+  BMFP_CUDA (cudaGetDevice (&dev));
+  BMFP_CUDA (cudaDeviceGetAttribute (&l2, cudaDevAttrL2CacheSize, dev));
+  const size_t flush_bytes = 2 * (size_t) std::max (l2, 1 << 20) + 64;
+  char *scratch = nullptr;
+  if (cudaMalloc (&scratch, flush_bytes) != cudaSuccess)
+    {
+      cudaGetLastError ();
+      scratch = nullptr; // time without flushing rather than fail
+    }
+  else
+    BMFP_CUDA (cudaMemsetAsync (scratch, 0, flush_bytes, s));
+  int *sink = scratch ? (int *) (scratch + flush_bytes - 64) : nullptr;
+  const size_t read_bytes = flush_bytes - 64;
   cudaEvent_t a, b;
   BMFP_CUDA (cudaEventCreate (&a));
   BMFP_CUDA (cudaEventCreate (&b));
@@ -422,24 +493,39 @@ int bmfp_matrix_autotune (bmfp_matrix_t m, const void *d_x, void *d_y, void *str
   int st = BMFP_SUCCESS;
   for (int i = 0; i < nc && st == BMFP_SUCCESS; i++)
     {
-      m->lanes = cand[i];
+      if (cand[i] == BMFP_LANES_COL_OWNER)
+        {
+          if (matrix_apply_lanes (m, cand[i], s) != BMFP_SUCCESS)
+            continue; // no room for the copy: not a candidate here
+        }
+      else
+        m->lanes = cand[i];
       for (int w = 0; w < 3 && st == BMFP_SUCCESS; w++)
         st = bmfp_matrix_spmv (m, d_x, d_y, stream);
       if (st != BMFP_SUCCESS)
         break;
-      cudaEventRecord (a, s);
-      const int reps = 10;
-      for (int r = 0; r < reps && st == BMFP_SUCCESS; r++)
-        st = bmfp_matrix_spmv (m, d_x, d_y, stream);
-      cudaEventRecord (b, s);
-      cudaError_t e = cudaEventSynchronize (b);
-      if (e != cudaSuccess)
-        {
-          st = cuda_fail (e, "autotune timing", __FILE__, __LINE__);
-          break;
-        }
+      const int reps = 5;
       float ms = 0;
-      cudaEventElapsedTime (&ms, a, b);
+      for (int r = 0; r < reps && st == BMFP_SUCCESS; r++)
+        {
+          if (scratch)
+            st = l2_flush (scratch, read_bytes, sink, s);
+          cudaEventRecord (a, s);
+          if (st == BMFP_SUCCESS)
+            st = bmfp_matrix_spmv (m, d_x, d_y, stream);
+          cudaEventRecord (b, s);
+          cudaError_t e = cudaEventSynchronize (b);
+          if (e != cudaSuccess)
+            {
+              st = cuda_fail (e, "autotune timing", __FILE__, __LINE__);
+              break;
+            }
+          float one = 0;
+          cudaEventElapsedTime (&one, a, b);
+          ms += one;
+        }
+      if (st != BMFP_SUCCESS)
+        break;
       if (ms < best)
         {
           best = ms;
@@ -448,7 +534,14 @@ int bmfp_matrix_autotune (bmfp_matrix_t m, const void *d_x, void *d_y, void *str
     }
   cudaEventDestroy (a);
   cudaEventDestroy (b);
-  m->lanes = st == BMFP_SUCCESS ? best_g : 0;
+  if (scratch)
+    {
+      cudaStreamSynchronize (s);
+      cudaFree (scratch);
+    }
+  const int keep = matrix_apply_lanes (m, st == BMFP_SUCCESS ? best_g : 0, s); // frees an unused copy
+  if (st == BMFP_SUCCESS)
+    st = keep;
   if (chosen_lanes)
     *chosen_lanes = m->lanes;
   return st;

@@ -19,7 +19,8 @@ struct bmfp_matrix_s
   int *d_row_ptr = nullptr;
   int *d_cols = nullptr;
   void *d_vals = nullptr;
-  int lanes = 0; // tuned lane count, 0 = heuristic
+  void *d_vals_cm = nullptr; // column-major copy of the blocks (BMFP_LANES_COL_OWNER only)
+  int lanes = 0;             // tuned lane count, 0 = heuristic
 };
 
 namespace bmfp
@@ -51,6 +52,13 @@ int convert_values (int src_dtype, int dst_dtype, int64_t n, const void *src, vo
                     cudaStream_t stream);
 // Valid lane counts for the native BCSR kernel at this block size, ascending.
 int native_lane_candidates (int dtype, int bs, int *out, int max_out);
+// Column-owner product over column-major blocks (bs in {4,8,16,32}), and the
+// row-major -> column-major copy it reads.
+int spmv_native_bcsr_colmajor (int dtype, int n_block_rows, int bs, const int *row_ptr, const int *cols,
+                               const void *vals_cm, const void *x, void *y, cudaStream_t stream);
+int transpose_blocks_device (int dtype, int64_t nnzb, int bs, const void *in, void *out, cudaStream_t stream);
+// Evicts L2 by reading `bytes` (> L2) of scratch; sink is a device int.
+int l2_flush (const void *scratch, size_t bytes, int *sink, cudaStream_t stream);
 } // namespace bmfp
 
 #define BMFP_CUDA(expr)                                                                  \

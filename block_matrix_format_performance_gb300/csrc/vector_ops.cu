@@ -21,6 +21,21 @@ unsigned grid_for (int64_t n)
     g = 152 * 32;
   return (unsigned) (g > 0 ? g : 1);
 }
+// Reads a scratch buffer larger than L2 so the next kernel finds none of its
+// data there; the sum is stored only under a condition the caller makes
+// impossible (sink_if == -1), so the reads cannot be optimised away.
+__global__ void l2_flush_kernel (const int4 *__restrict__ p, int64_t n, int sink_if, int *__restrict__ sink)
+{
+  int acc = 0;
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t) gridDim.x * blockDim.x)
+    {
+      const int4 v = p[i]; // default (evict-normal) policy: these lines displace the others
+      acc ^= v.x ^ v.y ^ v.z ^ v.w;
+    }
+  if (acc == sink_if)
+    *sink = acc;
+}
+
 template <typename S, typename D>
 __global__ void axpy_convert_kernel (int64_t n, double a, const S *__restrict__ src, D *__restrict__ dst)
 {
@@ -78,6 +93,16 @@ int scale_convert (int dst_dtype, int src_dtype, int64_t n, double a, const void
 }
 
 // Element type conversion on the device (FP64 -> FP32 rounds to nearest).
+int l2_flush (const void *scratch, size_t bytes, int *sink, cudaStream_t s)
+{
+  const int64_t n = (int64_t) (bytes / 16);
+  if (n == 0)
+    return BMFP_SUCCESS;
+  l2_flush_kernel<<<grid_for (n), 256, 0, s>>> ((const int4 *) scratch, n, -1, sink);
+  BMFP_LAUNCH_CHECK ();
+  return BMFP_SUCCESS;
+}
+
 int convert_values (int src_dtype, int dst_dtype, int64_t n, const void *src, void *dst,
                     cudaStream_t stream)
 {

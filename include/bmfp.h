@@ -151,6 +151,12 @@ BMFP_API int bmfp_bcsr_spmv (int dtype, int variant, int n_block_rows, int n_blo
  * line), or BMFP_LANES_ROW_OWNER (bs in {4,8,16,32}: one lane per scalar
  * row, no cross-lane reduction). Affects only BMFP_SPMV_BCSR_NATIVE. */
 #define BMFP_LANES_ROW_OWNER 64
+/* Matrix handles only (bmfp_matrix_set_lanes / bmfp_matrix_autotune): one lane
+ * per scalar row over a column-major copy of the blocks that the handle then
+ * keeps, so the lanes of a block read one contiguous column per load. The
+ * fastest FP64 mapping from bs 16 on (GB300's FP64 pipe busy most of the
+ * time); costs a second copy of the values in HBM. bs in {4,8,16,32}. */
+#define BMFP_LANES_COL_OWNER 65
 BMFP_API int bmfp_bcsr_spmv_native_ex (int dtype, int n_block_rows, int bs, int64_t nnzb,
                                        const int *d_row_ptr, const int *d_cols,
                                        const void *d_values, const void *d_x, void *d_y,
@@ -224,6 +230,10 @@ BMFP_API int bmfp_matrix_spmv (bmfp_matrix_t m, const void *d_x, void *d_y, void
  * the built-in heuristic. */
 BMFP_API int bmfp_matrix_autotune (bmfp_matrix_t m, const void *d_x, void *d_y, void *stream,
                                    int *chosen_lanes);
+/* Pin the native kernel's mapping for this handle (values as for
+ * bmfp_bcsr_spmv_native_ex, plus BMFP_LANES_COL_OWNER, which builds the
+ * column-major copy; any other value releases it). */
+BMFP_API int bmfp_matrix_set_lanes (bmfp_matrix_t m, int lanes, void *stream);
 
 /* ------------------------------------------------------------- BiCGStab ---
  * Replaces gpu_bicgstab<T,C> (gpu/bicgstab.h:10-16, gpu/bicgstab.cu:23-526):

@@ -260,3 +260,40 @@ def test_host_buffer_spmv_edges(lib, orc, cuda):
     with pytest.raises(bm.BmfpError) as e:
         bm.bcsr_spmv_host(np.array([0, 2], np.int32), np.zeros(1, np.int32), np.zeros(4), np.ones(2), 2)
     assert e.value.status == bm.ERROR_INVALID_VALUE
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("bs", [4, 8, 16, 32])
+def test_column_owner_mapping(lib, orc, cuda, bs, dtype):
+    """BMFP_LANES_COL_OWNER: the handle keeps a column-major copy of its blocks
+    and one lane per scalar row walks its columns; same parity bar as every
+    other mapping, on ragged rows with empty rows. Switching back releases
+    the copy and gives the row-major kernel's result again."""
+    import torch
+    nbr = 3000 if bs <= 8 else 600
+    rp, c, v = ragged_bcsr(nbr, nbr, bs, seed=bs + 50, dtype=dtype)
+    x = np.random.default_rng(bs).uniform(-1, 1, nbr * bs).astype(dtype)
+    m = bm.Matrix.from_bcsr(rp, c, v, bs)
+    dx = dev(x)
+    dy = torch.empty_like(dx)
+    crp, cc, cv = orc.bcsr_to_csr(rp, c, v, bs)
+    y_ref = orc.csr_spmv(crp, cc, cv, x, threads=8)
+    tol = spmv_tolerance(orc, crp, cc, cv, x, dtype)
+    m.set_lanes(bm.LANES_COL_OWNER)
+    m.spmv(dx, dy)
+    assert np.all(np.abs(dy.cpu().numpy() - y_ref) <= tol)
+    m.set_lanes(0)
+    m.spmv(dx, dy)
+    assert np.all(np.abs(dy.cpu().numpy() - y_ref) <= tol)
+    lanes = m.autotune(dx, dy)  # may pick the column owner again
+    m.spmv(dx, dy)
+    assert np.all(np.abs(dy.cpu().numpy() - y_ref) <= tol), lanes
+    m.close()
+
+
+def test_column_owner_rejected_where_it_does_not_apply(lib, cuda):
+    rp, c, v = ragged_bcsr(100, 100, 3, seed=1, dtype=np.float64)
+    m = bm.Matrix.from_bcsr(rp, c, v, 3)
+    with pytest.raises(bm.BmfpError):
+        m.set_lanes(bm.LANES_COL_OWNER)
+    m.close()
