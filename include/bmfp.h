@@ -232,7 +232,9 @@ BMFP_API int bmfp_matrix_autotune (bmfp_matrix_t m, const void *d_x, void *d_y, 
                                    int *chosen_lanes);
 /* Pin the native kernel's mapping for this handle (values as for
  * bmfp_bcsr_spmv_native_ex, plus BMFP_LANES_COL_OWNER, which builds the
- * column-major copy; any other value releases it). */
+ * column-major copy; any other value releases it). Like bmfp_matrix_autotune
+ * it changes the handle: do not call either while another thread multiplies
+ * with the same handle. */
 BMFP_API int bmfp_matrix_set_lanes (bmfp_matrix_t m, int lanes, void *stream);
 
 /* ------------------------------------------------------------- BiCGStab ---
