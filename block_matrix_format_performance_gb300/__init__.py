@@ -221,6 +221,13 @@ def bcsr_spmv_native(row_ptr, cols, vals, x, y, bs, lanes=0, stream=None):
     return y
 
 
+def bcsr_spmv_colmajor(row_ptr, cols, vals_colmajor, x, y, bs, stream=None):
+    """Column-owner product on device arrays with column-major blocks."""
+    check(load().bmfp_bcsr_spmv_colmajor(dtype_enum(vals_colmajor.dtype), row_ptr.numel() - 1, bs, cols.numel(),
+                                         _p(row_ptr), _p(cols), _p(vals_colmajor), _p(x), _p(y), _stream(stream)))
+    return y
+
+
 def csr_spmv(variant, row_ptr, cols, vals, x, y, n_cols=None, stream=None):
     n = row_ptr.numel() - 1
     check(load().bmfp_csr_spmv(dtype_enum(vals.dtype), variant, n, n_cols if n_cols is not None else x.numel(),

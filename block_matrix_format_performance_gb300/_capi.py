@@ -36,6 +36,8 @@ SIGNATURES = {
     "bmfp_bcsr_native_default_lanes": (c_int, [c_int, c_int, c_double]),
     "bmfp_mm_read_csr": (c_int, [ctypes.c_char_p, c_int, P(c_int), P(c_int), P(c_int64), c_void_p, c_void_p,
                                  c_void_p]),
+    "bmfp_bcsr_spmv_colmajor": (c_int, [c_int, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
+                                        c_void_p, c_void_p]),
     "bmfp_matrix_set_lanes": (c_int, [c_void_p, c_int, c_void_p]),
     "bmfp_measure_fma_peak": (c_int, [c_int, P(c_double), c_void_p]),
     "bmfp_bcsr_spmv_host": (c_int, [c_int, c_int, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_void_p,

@@ -177,6 +177,16 @@ int bmfp_bcsr_spmv_native_ex (int dtype, int n_block_rows, int bs, int64_t nnzb,
                            lanes, as_stream (stream));
 }
 
+int bmfp_bcsr_spmv_colmajor (int dtype, int nbr, int bs, int64_t nnzb, const int *d_row_ptr, const int *d_cols,
+                              const void *d_vals_cm, const void *d_x, void *d_y, void *stream)
+{
+  if (!dtype_ok (dtype) || nbr < 0 || nnzb < 0)
+    return fail (BMFP_ERROR_INVALID_VALUE, "invalid arguments");
+  if (nbr > 0 && (!d_row_ptr || !d_x || !d_y || (nnzb > 0 && (!d_cols || !d_vals_cm))))
+    return fail (BMFP_ERROR_INVALID_VALUE, "null device array");
+  return spmv_native_bcsr_colmajor (dtype, nbr, bs, d_row_ptr, d_cols, d_vals_cm, d_x, d_y, as_stream (stream));
+}
+
 int bmfp_bcsr_native_default_lanes (int dtype, int bs, double avg_blocks_per_row)
 {
   if (!dtype_ok (dtype) || bs < 1)

@@ -162,6 +162,14 @@ BMFP_API int bmfp_bcsr_spmv_native_ex (int dtype, int n_block_rows, int bs, int6
                                        const void *d_values, const void *d_x, void *d_y,
                                        int lanes_per_block_row, void *stream);
 BMFP_API int bmfp_bcsr_native_default_lanes (int dtype, int bs, double avg_blocks_per_row);
+/* The column-owner product (BMFP_LANES_COL_OWNER) on caller arrays whose
+ * blocks are already column-major (the transpose_blocks layout the
+ * reference's column-major variants take, gpu/gpu_matrix_multiplier.cu:
+ * 341-400). bs in {4,8,16,32}. The fastest FP64 product from bs 8 on. */
+BMFP_API int bmfp_bcsr_spmv_colmajor (int dtype, int n_block_rows, int bs, int64_t nnzb,
+                                      const int *d_row_ptr, const int *d_cols,
+                                      const void *d_values_colmajor, const void *d_x, void *d_y,
+                                      void *stream);
 
 /* Measured FMA throughput of the current device in GFLOP/s (2 flop per FMA)
  * for dtype R64F or R32F: a few milliseconds of independent FMA chains on

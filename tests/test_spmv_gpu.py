@@ -297,3 +297,19 @@ def test_column_owner_rejected_where_it_does_not_apply(lib, cuda):
     with pytest.raises(bm.BmfpError):
         m.set_lanes(bm.LANES_COL_OWNER)
     m.close()
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("bs", [4, 8, 16, 32])
+def test_column_owner_on_caller_arrays(lib, orc, cuda, bs, dtype):
+    """bmfp_bcsr_spmv_colmajor on the transpose_blocks layout the caller holds."""
+    import torch
+    nbr = 2000 if bs <= 8 else 400
+    rp, c, v = ragged_bcsr(nbr, nbr, bs, seed=bs + 70, dtype=dtype)
+    x = np.random.default_rng(bs + 1).uniform(-1, 1, nbr * bs).astype(dtype)
+    vt = bm.transpose_blocks(rp, v, bs)
+    dy = torch.empty(nbr * bs, dtype=torch.float64 if dtype == np.float64 else torch.float32, device="cuda")
+    bm.bcsr_spmv_colmajor(dev(rp), dev(c), dev(vt), dev(x), dy, bs)
+    crp, cc, cv = orc.bcsr_to_csr(rp, c, v, bs)
+    y_ref = orc.csr_spmv(crp, cc, cv, x, threads=8)
+    assert np.all(np.abs(dy.cpu().numpy() - y_ref) <= spmv_tolerance(orc, crp, cc, cv, x, dtype))
