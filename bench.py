@@ -102,7 +102,8 @@ def parse_args():
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--max-iters", type=int, default=200000)
     ap.add_argument("--repeats", type=int, default=3)
-    ap.add_argument("--ctas-per-sm", type=int, default=0, help="solve: persistent grid of the solver (0 = default)")
+    ap.add_argument("--ctas-per-sm", type=int, default=0,
+                    help="solve / serve: persistent grid of the single-system solver (0 = default)")
     return ap.parse_args()
 
 
@@ -741,6 +742,8 @@ def run_serve(args):
         kw["cluster_size"] = args.cluster_size
     if args.threads_per_cta is not None:
         kw["threads_per_cta"] = args.threads_per_cta
+    if args.ctas_per_sm:
+        kw["ctas_per_sm"] = args.ctas_per_sm
     srv = bm.Server(args.precision, tol=args.tol, max_iters=args.max_iters, **kw)
     # warm-up: one small request
     w = np.zeros(mats[min(mats)].rows)

@@ -344,10 +344,13 @@ PRECOND_NONE, PRECOND_JACOBI = 0, 1
 _PRECISIONS = {"fp64": SOLVE_FP64, "fp32": SOLVE_FP32, "mixed": SOLVE_MIXED}
 
 
-def solver_options(**kw) -> SolverOptions:
-    """bmfp_solver_options with the library defaults, then keyword overrides."""
+def solver_options(base=None, **kw) -> SolverOptions:
+    """bmfp_solver_options: the library defaults (or `base`), then keyword overrides."""
     o = SolverOptions()
-    load().bmfp_solver_options_init(ctypes.byref(o))
+    if base is not None:
+        ctypes.pointer(o)[0] = base
+    else:
+        load().bmfp_solver_options_init(ctypes.byref(o))
     for k, v in kw.items():
         if k == "precision" and isinstance(v, str):
             v = _PRECISIONS[v]
@@ -453,7 +456,8 @@ class Server:
                   "wide_lanes"):
             if k in kw:
                 setattr(o, k, kw.pop(k))
-        o.solver = solver_options(precision=precision, tolerance=tol, max_iterations=max_iters, **kw)
+        # start from the server's own solver defaults (one CTA per SM for the whole-GPU lanes)
+        o.solver = solver_options(o.solver, precision=precision, tolerance=tol, max_iterations=max_iters, **kw)
         self.options = o
         h = ctypes.c_void_p()
         check(load().bmfp_server_create(ctypes.byref(h), ctypes.byref(o)))

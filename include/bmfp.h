@@ -375,8 +375,9 @@ typedef struct bmfp_server_options
   int cluster_size;            /* CTAs per system team (default 4) */
   int threads_per_cta;         /* default 512 */
   int64_t wide_threshold_rows; /* larger requests use the whole-GPU engine (default 200000) */
-  int wide_lanes;              /* whole-GPU solves run concurrently (default 4) */
-  bmfp_solver_options solver;  /* precision, tolerance, limits; no preconditioner */
+  int wide_lanes;              /* whole-GPU solves run concurrently (default 8) */
+  bmfp_solver_options solver;  /* precision, tolerance, limits; no preconditioner;
+                                  ctas_per_sm defaults to 1 here (eight lanes share the SMs) */
 } bmfp_server_options;
 
 typedef struct bmfp_server_stats
