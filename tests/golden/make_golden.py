@@ -84,8 +84,8 @@ def main():
                 fa, fb = os.path.join(tmp, "a.bin"), os.path.join(tmp, "b.bin")
                 a.tofile(fa)
                 b.tofile(fb)
-                verdict = run("compare", dt, a.size, fa, fb).strip()
-                cases.append({"dtype": dt, "a": a.tolist(), "b": b.tolist(), "flagged": verdict == "FLAGGED"})
+                flag = run("compare", dt, a.size, fa, fb).strip()
+                cases.append({"dtype": dt, "a": a.tolist(), "b": b.tolist(), "flagged": flag == "FLAGGED"})
         with open(os.path.join(HERE, "compare_results.json"), "w") as f:
             json.dump(cases, f)
 
