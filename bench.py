@@ -20,6 +20,10 @@ construction: the reference has no dataset, only generated matrices.
                download, handle release — copies inside the timed region.
   roofline     the dominant product (largest share of device time) against
                MEASURED_PEAKS.json's HBM copy bandwidth.
+  read floor   per product (per_case[*].read_floor_us): a plain streaming read
+               of the same bytes after the same flush (bmfp_stream_read), the
+               size-matched floor that launch ramp and DRAM latency set for
+               the small products.
   cpu_baseline the oracle's restatement of the reference CPU loop
                (main.cpp:36-45, one thread) on the first rows of every matrix.
 
@@ -226,6 +230,32 @@ def peaks():
         return FALLBACK_HBM_GBS, "fallback"
 
 
+def read_floor_us(byte_counts, flush, stream, reps=20):
+    """Device time of a plain streaming read of each byte count (bmfp_stream_read),
+    timed exactly like the products: L2 flushed, then CUDA events around one
+    launch. The size-matched floor of a small product: launch ramp, first DRAM
+    round trips and tail cost every kernel a few microseconds."""
+    import torch
+    import block_matrix_format_performance_gb300 as bm
+    buf = torch.empty((max(byte_counts) + 15) // 16 * 4, dtype=torch.float32, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = []
+    for nb in byte_counts:
+        nb16 = (nb + 15) // 16 * 16
+        total = 0.0
+        for r in range(reps + 2):
+            flush()
+            e0.record(stream)
+            bm.stream_read(buf, nb16, stream=stream)
+            e1.record(stream)
+            e1.synchronize()
+            if r >= 2:
+                total += e0.elapsed_time(e1)
+        out.append(total / reps * 1e3)
+    del buf
+    return out
+
+
 def committed_traffic(kernel_key):
     """dram bytes per launch of the dominant kernel from the committed ncu
     summary (profiles/*.md line `traffic <key>: <bytes>`), or None."""
@@ -320,12 +350,15 @@ def run_ours(args):
     # The second roofline of FP64 products: GB300's FP64 FMA rate, measured
     # here (one FMA per value, so at most bytes / (2 nnzb bs^2 / rate)).
     fp64_gflops = bm.measure_fma_peak(np.float64)
+    read_us = read_floor_us([cs["bytes"] for cs in cases], flush, stream)
     per_case = {}
     for i, cs in enumerate(cases):
         ms = per_case_ms[i] / args.steps
         gbs = cs["bytes"] / (ms * 1e-3) / 1e9
         per_case[f"bs{cs['bs']}_{cs['tag']}"] = {"gbs": round(gbs, 1), "us": round(ms * 1e3, 2),
-                                                  "mb": round(cs["bytes"] / 1e6, 1), "lanes": cs["lanes"]}
+                                                  "mb": round(cs["bytes"] / 1e6, 1), "lanes": cs["lanes"],
+                                                  "read_floor_us": round(read_us[i], 2),
+                                                  "of_read_floor": round(read_us[i] / (ms * 1e3), 3)}
         if cs["tag"] == "f64":
             bound = cs["bytes"] / (2.0 * cs["nnzb"] * cs["bs"] ** 2 / (fp64_gflops * 1e9)) / 1e9
             per_case[f"bs{cs['bs']}_{cs['tag']}"]["of_min_hbm_fp64_bound"] = round(gbs / min(bound, peaks()[0]), 3)

@@ -259,6 +259,13 @@ def measure_fma_peak(dtype=np.float64, stream=None) -> float:
     return g.value
 
 
+def stream_read(buf, nbytes=None, stream=None) -> None:
+    """Launch one plain streaming read of a device tensor (bmfp_stream_read):
+    time it like a product to get the size-matched read floor."""
+    n = buf.numel() * buf.element_size() if nbytes is None else int(nbytes)
+    check(load().bmfp_stream_read(ctypes.c_void_p(buf.data_ptr()), n, _stream(stream)))
+
+
 def native_default_lanes(dtype, bs, avg_blocks_per_row) -> int:
     return load().bmfp_bcsr_native_default_lanes(dtype_enum(dtype), bs, float(avg_blocks_per_row))
 

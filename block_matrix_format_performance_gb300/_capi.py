@@ -40,6 +40,7 @@ SIGNATURES = {
                                         c_void_p, c_void_p]),
     "bmfp_matrix_set_lanes": (c_int, [c_void_p, c_int, c_void_p]),
     "bmfp_measure_fma_peak": (c_int, [c_int, P(c_double), c_void_p]),
+    "bmfp_stream_read": (c_int, [c_void_p, ctypes.c_size_t, c_void_p]),
     "bmfp_bcsr_spmv_host": (c_int, [c_int, c_int, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
                                     c_void_p, c_int, c_void_p]),
     "bmfp_matrix_create_bcsr": (c_int, [P(c_void_p), c_int, c_int, c_int, c_int, c_int64, c_void_p,

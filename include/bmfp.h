@@ -177,6 +177,12 @@ BMFP_API int bmfp_bcsr_spmv_colmajor (int dtype, int n_block_rows, int bs, int64
  * so at most 4 bytes per FP64 flop); bench.py reports both rooflines. */
 BMFP_API int bmfp_measure_fma_peak (int dtype, double *gflops, void *stream);
 
+/* Launches one plain streaming read of `bytes` device bytes at d_buf (16-byte
+ * aligned, bytes a multiple of 16) on `stream`, for the caller to time like a
+ * product: the size-matched floor of a small SpMV, whose launch ramp, first
+ * DRAM round trips and tail no kernel avoids (no reference counterpart). */
+BMFP_API int bmfp_stream_read (const void *d_buf, size_t bytes, void *stream);
+
 /* One-shot product on HOST buffers: y = A x with the BCSR arrays (row-major
  * blocks; bs = 1 is CSR), x and y all in host memory, the call returning when
  * h_y holds the result. Replaces what each gpu_bcsr_spmv / gpu_csr_spmv call

@@ -62,3 +62,16 @@ def test_fma_peak_probe(cuda):
     f64 = bm.measure_fma_peak(np.float64)
     f32 = bm.measure_fma_peak(np.float32)
     assert 50.0 < f64 < f32  # GFLOP/s; FP32 FMA is far faster than FP64 on GB300
+
+
+def test_stream_read_floor(cuda):
+    import torch
+    import block_matrix_format_performance_gb300 as bm
+    buf = torch.ones(1 << 20, dtype=torch.float32, device="cuda")
+    bm.stream_read(buf)  # 4 MB, the whole buffer
+    bm.stream_read(buf, 0)
+    torch.cuda.synchronize()
+    with pytest.raises(bm.BmfpError):  # not a multiple of 16 bytes
+        bm.stream_read(buf, 24)
+    with pytest.raises(bm.BmfpError):  # misaligned start
+        bm.stream_read(buf[1:], 16)
