@@ -209,9 +209,14 @@ struct Scal
 // over the best seen, or turns non-finite, ends the run as a breakdown. Each
 // thread copies and restores the elements it also updates, so the copies
 // need no barrier of their own.
+//
+// stall > 0 (inner solves of mixed precision): a run whose recursive
+// residual has not halved after `stall` iterations ends with status 4; its
+// caller discards such a run, so the remaining iterations would be spent on
+// a result that is thrown away.
 template <typename T, int OP>
 __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, const T *rhs, T *x, bool zero_x,
-                                   double tol, int max_it, double norm_ref, T *snap = nullptr)
+                                   double tol, int max_it, double norm_ref, T *snap = nullptr, int stall = 0)
 {
   using Op = TeamOp<T, OP>;
   const TeamIdx ix = team_index<Op::G> (cl);
@@ -235,6 +240,7 @@ __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, c
     sc.a = norm_ref > 0.0 ? norm_ref : sqrt (out1[0]);
   __syncthreads ();
   const double nb = sc.a;
+  const double rr_start = out1[0];
   double rho = out1[0], rr = out1[0]; // rh == r at the start
   double rho_prev = 1.0, alpha = 1.0, omega = 1.0;
   // Team-uniform (every thread holds the same rr), so no broadcast needed.
@@ -259,6 +265,8 @@ __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, c
             st = 1;
           else if (o.iters >= max_it)
             st = 2;
+          else if (stall > 0 && o.iters >= stall && best_rr > 0.25 * rr_start)
+            st = 4;
           else if (rho == 0.0 || omega == 0.0 || !isfinite (rho) || !(rr <= 1e16 * best_rr))
             st = 3;
           else
@@ -526,7 +534,8 @@ __device__ void solve_system (cg::cluster_group &cl, const BatchDesc &D, const B
             r32[i] = (float) (r64[i] * inv);
           cl.sync ();
           const int cap = min (P.inner_max, P.max_it - iters32 - iters64);
-          const SolveOut o = team_bicgstab<float, OP> (cl, S32, r32, x32, true, P.inner_tol, cap, -1.0);
+          const SolveOut o = team_bicgstab<float, OP> (cl, S32, r32, x32, true, P.inner_tol, cap, -1.0,
+                                                       nullptr, P.inner_stall);
           iters32 += o.iters;
           refinements = k + 1;
           if (!(o.rec_rel < 0.5))
@@ -768,6 +777,7 @@ int BatchEngine::launch (cudaStream_t s, int max_it_override)
   P.max_it = max_it_override > 0 ? max_it_override : opts_.max_iterations;
   P.inner_tol = opts_.inner_tolerance;
   P.inner_max = opts_.inner_max_iterations;
+  P.inner_stall = opts_.inner_stall_iterations;
   P.max_ref = opts_.max_refinements;
   P.fallback = opts_.fallback_fp64;
   BMFP_CUDA (cudaMemsetAsync (d_counter_, 0, sizeof (int), s));

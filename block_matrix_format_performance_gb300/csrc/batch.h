@@ -46,6 +46,7 @@ struct BatchParams
   int max_it;
   double inner_tol;
   int inner_max;
+  int inner_stall;
   int max_ref;
   int fallback;
 };

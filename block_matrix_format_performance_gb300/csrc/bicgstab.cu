@@ -840,7 +840,7 @@ __global__ void stop_kernel (DevState *st)
 }
 } // namespace
 
-int WideEngine::run (cudaStream_t s, DevState *out, void *d_snap, double *snap_rr)
+int WideEngine::run (cudaStream_t s, DevState *out, void *d_snap, double *snap_rr, int stall)
 {
   // Keep one graph in flight while the host inspects the previous one.
   long k = 0;
@@ -872,7 +872,8 @@ int WideEngine::run (cudaStream_t s, DevState *out, void *d_snap, double *snap_r
               snap_k = k;
               snap_at = h.rr;
             }
-          if (!stopping && !(h.rr <= 1e16 * best))
+          const bool stalled = stall > 0 && h.iter >= stall && best > 0.25 * h.norm_b * h.norm_b;
+          if (!stopping && (!(h.rr <= 1e16 * best) || stalled))
             {
               stop_kernel<<<1, 1, 0, s>>> (state_);
               BMFP_LAUNCH_CHECK ();

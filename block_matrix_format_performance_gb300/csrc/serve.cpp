@@ -304,6 +304,7 @@ int launch_micro_batch (bmfp_server_s *sv, std::vector<Request *> &reqs, int str
   P.max_it = o.max_iterations;
   P.inner_tol = o.inner_tolerance;
   P.inner_max = o.inner_max_iterations;
+  P.inner_stall = o.inner_stall_iterations;
   P.max_ref = o.max_refinements;
   P.fallback = o.fallback_fp64;
   const int clusters = std::max (1, std::min (n, sv->cluster_cap));
@@ -592,7 +593,7 @@ int bmfp_server_create (bmfp_server_t *out, const bmfp_server_options *opts)
   if (opts)
     o = *opts;
   if (o.max_in_flight < 1 || o.max_batch < 1 || o.streams < 1 || o.streams > 64 || o.hbm_budget_bytes == 0
-      || o.wide_lanes < 1 || o.wide_lanes > 16)
+      || o.wide_lanes < 1 || o.wide_lanes > 16 || o.solver.inner_stall_iterations < 0)
     return fail (BMFP_ERROR_INVALID_VALUE, "invalid server options");
   if (o.solver.preconditioner != BMFP_PRECOND_NONE)
     return fail (BMFP_ERROR_NOT_SUPPORTED, "the server takes no preconditioner");

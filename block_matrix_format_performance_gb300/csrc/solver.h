@@ -56,13 +56,15 @@ public:
   // whose last run belonged to an earlier one); -1 keeps counting.
   int start_residual (const void *d_r, double tol, int max_iter_total, double norm_b,
                       cudaStream_t stream, int iter0 = -1);
-  // Run graph chunks until the device sets done; returns the final state.
-  // Runs graphs until the device sets done. With d_snapshot, x is copied
-  // there each time the recursive residual has fallen 4x below the last copy
-  // (and below snapshot_rr on entry), and *snapshot_rr receives the (r, r) of
-  // the copy; a residual that grows 1e8-fold over the best seen, or turns
-  // non-finite, stops the run as a breakdown.
-  int run (cudaStream_t stream, DevState *out, void *d_snapshot = nullptr, double *snapshot_rr = nullptr);
+  // Runs graphs until the device sets done; returns the final state. With
+  // d_snapshot, x is copied there each time the recursive residual has
+  // fallen 4x below the last copy (and below snapshot_rr on entry), and
+  // *snapshot_rr receives the (r, r) of the copy; a residual that grows
+  // 1e8-fold over the best seen, or turns non-finite, stops the run as a
+  // breakdown, and so does (stall > 0) a residual that has not halved after
+  // `stall` iterations.
+  int run (cudaStream_t stream, DevState *out, void *d_snapshot = nullptr, double *snapshot_rr = nullptr,
+           int stall = 0);
   // r = b - A x, returns ||r||^2 and ||b||^2 (synchronises the stream).
   int true_residual (const void *d_b, void *d_r, double *rr, double *bb, cudaStream_t stream);
 

@@ -254,7 +254,7 @@ int solve_mixed (bmfp_solver_s *sv, const void *d_b, bmfp_solve_info *info, cuda
       const int cap = std::min (o.inner_max_iterations, o.max_iterations - iters64 - iters32);
       rc = e32.start_zero (r32, o.inner_tolerance, cap, s);
       if (rc == BMFP_SUCCESS)
-        rc = e32.run (s, &st);
+        rc = e32.run (s, &st, nullptr, nullptr, o.inner_stall_iterations);
       if (rc != BMFP_SUCCESS)
         return rc;
       iters32 += st.iter;
@@ -293,6 +293,7 @@ void bmfp_solver_options_init (bmfp_solver_options *o)
   o->fallback_fp64 = 1;
   o->iterations_per_graph = 16;
   o->ctas_per_sm = 4;
+  o->inner_stall_iterations = 64;
 }
 
 int bmfp_solver_create (bmfp_solver_t *out, bmfp_matrix_t A, const bmfp_solver_options *opts,
@@ -310,7 +311,7 @@ int bmfp_solver_create (bmfp_solver_t *out, bmfp_matrix_t A, const bmfp_solver_o
   if (o.preconditioner != BMFP_PRECOND_NONE && o.preconditioner != BMFP_PRECOND_JACOBI)
     return fail (BMFP_ERROR_INVALID_VALUE, "invalid preconditioner %d", o.preconditioner);
   if (!(o.tolerance > 0) || o.max_iterations < 0 || o.iterations_per_graph < 1 || o.ctas_per_sm < 1
-      || o.ctas_per_sm > 8)
+      || o.ctas_per_sm > 8 || o.inner_stall_iterations < 0)
     return fail (BMFP_ERROR_INVALID_VALUE, "invalid tolerance or iteration limits");
   if (o.precision == BMFP_SOLVE_MIXED && A->dtype != BMFP_R64F)
     return fail (BMFP_ERROR_INVALID_VALUE, "mixed precision needs an FP64 matrix");
@@ -438,8 +439,9 @@ int bmfp_batch_create (bmfp_batch_t *out, int n, const bmfp_matrix_t *mats, cons
   bmfp_solver_options_init (&o);
   if (opts)
     o = *opts;
-  if (o.precision < BMFP_SOLVE_FP64 || o.precision > BMFP_SOLVE_MIXED || !(o.tolerance > 0))
-    return fail (BMFP_ERROR_INVALID_VALUE, "invalid precision or tolerance");
+  if (o.precision < BMFP_SOLVE_FP64 || o.precision > BMFP_SOLVE_MIXED || !(o.tolerance > 0)
+      || o.inner_stall_iterations < 0)
+    return fail (BMFP_ERROR_INVALID_VALUE, "invalid precision, tolerance or stall limit");
   if (o.preconditioner != BMFP_PRECOND_NONE)
     return fail (BMFP_ERROR_NOT_SUPPORTED, "batched solves take no preconditioner");
   std::unique_ptr<bmfp_batch_s> b (new (std::nothrow) bmfp_batch_s);

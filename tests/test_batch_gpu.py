@@ -148,3 +148,24 @@ def test_mixed_block_sizes_and_csr_systems(lib, cuda):
     info = batch.solve(d_b, d_x)[0]
     assert info["status"] == bm.SUCCESS
     assert np.linalg.norm(b - sp.csr_matrix((cv, cc, crp)) @ d_x[0].cpu().numpy()) / np.linalg.norm(b) < 1e-10
+
+
+def test_inner_stall_window_keeps_results_and_cuts_fp32_work(lib, cuda):
+    # FP32 inner solves cannot progress on the elasticity operator: a run that
+    # has not halved its residual within the window is abandoned early. The
+    # solves still reach the tolerance through the FP64 finish.
+    systems = q4_systems([(100, 25), (64, 16), (40, 10)])
+    _, infos0 = run_batch(systems, "mixed", (4, 256), max_iters=50000, inner_stall_iterations=0)
+    xs, infos16 = run_batch(systems, "mixed", (4, 256), max_iters=50000, inner_stall_iterations=16)
+    for (rp, c, v, rhs, bs), x, info in zip(systems, xs, infos16):
+        K = csr_of(rp, c, v, bs)
+        assert info["status"] == bm.SUCCESS, info
+        assert np.linalg.norm(rhs - K @ x) / np.linalg.norm(rhs) < 1e-10
+    assert sum(i["iterations_fp32"] for i in infos16) <= sum(i["iterations_fp32"] for i in infos0)
+    rp, c, v, _, bs = systems[0]
+    m = bm.Matrix.from_bcsr(rp, c, v, bs)
+    try:
+        with pytest.raises(bm.BmfpError):
+            bm.Batch([m], "mixed", inner_stall_iterations=-1)
+    finally:
+        m.close()

@@ -96,3 +96,11 @@ def test_oracle_is_not_linked_into_the_product(lib):
             if f.endswith((".py", ".cu", ".cpp", ".h", ".cuh")):
                 text = open(os.path.join(dp, f)).read()
                 assert "oracle" not in text.lower().replace("the oracle", ""), f
+
+
+def test_solver_option_defaults(lib):
+    o = bm.solver_options()
+    assert o.precision == bm.SOLVE_FP64 and o.tolerance == 1e-10
+    assert o.inner_tolerance == 1e-4 and o.inner_max_iterations == 1000
+    assert o.ctas_per_sm == 4 and o.inner_stall_iterations == 64
+    assert bm.solver_options(inner_stall_iterations=0).inner_stall_iterations == 0
