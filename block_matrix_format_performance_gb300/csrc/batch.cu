@@ -210,10 +210,11 @@ struct Scal
 // thread copies and restores the elements it also updates, so the copies
 // need no barrier of their own.
 //
-// stall > 0 (inner solves of mixed precision): a run whose recursive
-// residual has not halved after `stall` iterations ends with status 4; its
-// caller discards such a run, so the remaining iterations would be spent on
-// a result that is thrown away.
+// stall > 0 (inner solves of mixed precision): a run whose best recursive
+// residual has not halved within a window of `stall` iterations (counted
+// from the start or from the last halving) ends with status 4. The caller
+// keeps such a run only if it halved at least once, so the iterations of a
+// plateau would be spent on a result the next refinement step redoes.
 template <typename T, int OP>
 __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, const T *rhs, T *x, bool zero_x,
                                    double tol, int max_it, double norm_ref, T *snap = nullptr, int stall = 0)
@@ -240,8 +241,9 @@ __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, c
     sc.a = norm_ref > 0.0 ? norm_ref : sqrt (out1[0]);
   __syncthreads ();
   const double nb = sc.a;
-  const double rr_start = out1[0];
   double rho = out1[0], rr = out1[0]; // rh == r at the start
+  double mark_rr = out1[0];           // best (r, r) at the last halving
+  int mark_it = 0;
   double rho_prev = 1.0, alpha = 1.0, omega = 1.0;
   // Team-uniform (every thread holds the same rr), so no broadcast needed.
   double best_rr = rr, snap_rr = INFINITY;
@@ -249,6 +251,11 @@ __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, c
     {
       if (rr < best_rr)
         best_rr = rr;
+      if (best_rr <= 0.25 * mark_rr)
+        {
+          mark_rr = best_rr;
+          mark_it = o.iters;
+        }
       if (snap && rr < 0.25 * snap_rr)
         {
           for (int64_t i = ix.elem0; i < S.n; i += ix.elem_stride)
@@ -265,7 +272,7 @@ __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, c
             st = 1;
           else if (o.iters >= max_it)
             st = 2;
-          else if (stall > 0 && o.iters >= stall && best_rr > 0.25 * rr_start)
+          else if (stall > 0 && o.iters - mark_it >= stall)
             st = 4;
           else if (rho == 0.0 || omega == 0.0 || !isfinite (rho) || !(rr <= 1e16 * best_rr))
             st = 3;
@@ -483,7 +490,8 @@ __device__ void solve_system (cg::cluster_group &cl, const BatchDesc &D, const B
   else
     {
       // MIXED: FP32 inner solves, FP64 residual, update and norm; an FP64
-      // finish (with restarts) from the current x when a step gains < 4x.
+      // finish (with restarts) when a step gains < 4x, from the current x or,
+      // when the FP32 steps gained less than 100x in all, from x = 0.
       TeamSys<float> S32{ D.nbr, D.bs, D.n, D.rp, D.cols, D.vals32,
                           D.w32, D.w32 + D.n, D.w32 + 2 * D.n, D.w32 + 3 * D.n, D.w32 + 4 * D.n, D.w32 + 5 * D.n };
       float *x32 = D.w32 + 6 * D.n, *r32 = D.w32 + 7 * D.n;
@@ -519,7 +527,13 @@ __device__ void solve_system (cg::cluster_group &cl, const BatchDesc &D, const B
                 }
               fallback = 1;
               const double nb = rel > 0 ? sh_scale / rel : 0.0; // ||b||
-              const Fp64Result f = fp64_restarted<OP> (cl, S64, D, P, false, P.max_it - iters32, nb, r64);
+              // FP32 steps that gained less than 100x leave an iterate from
+              // which FP64 BiCGStab measured 1.1-1.8x the iterations it needs
+              // from x = 0 (elasticity family): start over from zero then,
+              // exactly as the FP64 solve does (same ||b||, same bits).
+              const bool fresh = rel > 1e-2;
+              const Fp64Result f
+                = fp64_restarted<OP> (cl, S64, D, P, fresh, P.max_it - iters32, fresh ? -1.0 : nb, r64);
               iters64 += f.iters;
               status = f.status;
               restarts = f.restarts;

@@ -849,6 +849,8 @@ int WideEngine::run (cudaStream_t s, DevState *out, void *d_snap, double *snap_r
   double best = INFINITY;                              // smallest (r, r) polled
   double snap_at = snap_rr ? *snap_rr : INFINITY;      // (r, r) of the last copy
   long snap_k = -1;                                    // graph whose end the copy holds
+  double mark = INFINITY;                              // best (r, r) at the last halving
+  int mark_it = 0;                                     // iteration of that halving
   bool stopping = false;
   for (;; k++)
     {
@@ -872,7 +874,14 @@ int WideEngine::run (cudaStream_t s, DevState *out, void *d_snap, double *snap_r
               snap_k = k;
               snap_at = h.rr;
             }
-          const bool stalled = stall > 0 && h.iter >= stall && best > 0.25 * h.norm_b * h.norm_b;
+          if (mark == INFINITY)
+            mark = h.norm_b * h.norm_b;
+          if (best <= 0.25 * mark)
+            {
+              mark = best;
+              mark_it = h.iter;
+            }
+          const bool stalled = stall > 0 && h.iter - mark_it >= stall;
           if (!stopping && (!(h.rr <= 1e16 * best) || stalled))
             {
               stop_kernel<<<1, 1, 0, s>>> (state_);

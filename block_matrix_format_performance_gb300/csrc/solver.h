@@ -61,8 +61,8 @@ public:
   // fallen 4x below the last copy (and below snapshot_rr on entry), and
   // *snapshot_rr receives the (r, r) of the copy; a residual that grows
   // 1e8-fold over the best seen, or turns non-finite, stops the run as a
-  // breakdown, and so does (stall > 0) a residual that has not halved after
-  // `stall` iterations.
+  // breakdown, and so does (stall > 0) a best residual that has not halved
+  // within `stall` iterations of the start or of its last halving.
   int run (cudaStream_t stream, DevState *out, void *d_snapshot = nullptr, double *snapshot_rr = nullptr,
            int stall = 0);
   // r = b - A x, returns ||r||^2 and ||b||^2 (synchronises the stream).

@@ -292,9 +292,10 @@ typedef struct bmfp_solver_options
   int ctas_per_sm;          /* persistent grid of the single-system solver: CTAs of 256
                                threads per SM (default 4); the grid fixes the summation
                                order, so results are bitwise repeatable for a given value */
-  int inner_stall_iterations; /* MIXED: an FP32 inner solve whose recursive residual has not
-                               halved after this many iterations is abandoned (it would be
-                               discarded at its end anyway); 0 = never */
+  int inner_stall_iterations; /* MIXED: an FP32 inner solve whose best recursive residual
+                               has not halved within this many iterations (of its start or
+                               of its last halving) is stopped there; it is applied if it
+                               halved at least once. 0 = never */
 } bmfp_solver_options;
 
 typedef struct bmfp_solve_info
