@@ -79,11 +79,14 @@ def parse_args():
     ap.add_argument("--dtypes", default=",".join(DTYPES))
     ap.add_argument("--n-block-rows", type=int, default=NBR,
                     help="block rows per matrix (smaller only for profiling captures)")
-    ap.add_argument("--workload", choices=("spmv", "solve", "batch", "serve", "ndiag"), default="spmv",
+    ap.add_argument("--workload", choices=("spmv", "solve", "batch", "serve", "ndiag", "bridge"), default="spmv",
                     help="spmv: the block-size sweep line (default); solve: one Q4 elasticity solve; "
                          "batch: 256 uneven Q4 systems in one persistent launch; serve: Poisson request "
                          "stream through the server; ndiag: every variant on gen_n_diag_bcsr matrices, "
-                         "written in the reference's result.json layout")
+                         "written in the reference's result.json layout; bridge: the Golden Gate truss "
+                         "through every format and main.cpp's Jacobi BiCGStab solve")
+    ap.add_argument("--bridge-main-span", type=float, default=128000.0,
+                    help="bridge: main span in metres (main.cpp:354 uses 128 km)")
     ap.add_argument("--results-json", default=None, help="ndiag: write {bs: {format: seconds}} here")
     ap.add_argument("--ndiag-rows", type=int, default=50_000, help="ndiag: block rows")
     ap.add_argument("--ndiag-dtype", default="f32", choices=("f32", "f64"))
@@ -846,6 +849,68 @@ def run_serve(args):
         "per_request_fp64": baseline}), flush=True)
 
 
+def measure_variants(rp, c, v, bs, x, runs, stream):
+    """Every SpMV format of the reference on one BCSR matrix (perform_measurements,
+    main.cpp:131-148): "CPU CSR" is the single-thread CPU loop (main.cpp:21-63)
+    through the oracle's restatement; each GPU format is checked against it
+    with compare_results' rule (sum (a-b)^2 / sum b^2 <= 1e-9,
+    measurement_class.h:58-87) and timed `runs` times between CUDA events.
+    Returns ({format: mean seconds}, worst compare_results error)."""
+    import torch
+
+    import block_matrix_format_performance_gb300 as bm
+    from oracle import oracle as orc
+    n = x.size
+    crp, cc, cv = bm.bcsr_to_csr(rp, c, v, bs)
+    vt = bm.transpose_blocks(rp, v, bs)
+    res = {}
+    y_ref = orc.csr_spmv(crp, cc, cv, x)
+    t0 = time.perf_counter()
+    for _ in range(runs):
+        orc.csr_spmv(crp, cc, cv, x)
+    res["CPU CSR"] = (time.perf_counter() - t0) / runs
+    d = {k: torch.from_numpy(a).cuda() for k, a in
+         (("rp", rp), ("c", c), ("v", v), ("vt", vt), ("crp", crp), ("cc", cc), ("cv", cv), ("x", x))}
+    dy = torch.empty(n, dtype=d["x"].dtype, device="cuda")
+    colown = v.dtype == np.float64 and bs in (8, 16, 32)
+    worst = 0.0
+    for var in range(bm.VARIANT_COUNT):
+        name = bm.variant_name(var)
+
+        def launch():
+            if bm.variant_is_csr(var):
+                bm.csr_spmv(var, d["crp"], d["cc"], d["cv"], d["x"], dy)
+            elif var == bm.BCSR_NATIVE and colown:
+                # as the C++ drop-in's gpu_bcsr_spmv runs the native format:
+                # the column owner on the caller's transposed blocks
+                bm.bcsr_spmv_colmajor(d["rp"], d["c"], d["vt"], d["x"], dy, bs)
+            else:
+                vals = d["vt"] if bm.variant_layout(var) == 1 else d["v"]
+                bm.bcsr_spmv(var, d["rp"], d["c"], vals, d["x"], dy, bs)
+        try:
+            launch()
+        except bm.BmfpError as e:
+            if e.status == bm.ERROR_NOT_SUPPORTED:
+                continue  # e.g. the power-of-two variant at other bs, as gpu_matrix_multiplier.cu:1226
+            raise
+        torch.cuda.synchronize()
+        y = dy.cpu().numpy()
+        err = float(np.sum((y.astype(np.float64) - y_ref) ** 2) / np.sum(y_ref.astype(np.float64) ** 2))
+        worst = max(worst, err)
+        if err > 1e-9:
+            raise SystemExit(f"{name} bs {bs}: compare_results error {err:.3e}")
+        tot = 0.0
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for _ in range(runs):
+            e0.record(stream)
+            launch()
+            e1.record(stream)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1) * 1e-3
+        res[name] = tot / runs
+    return res, worst
+
+
 def run_ndiag(args, sizes=(2, 4, 8, 16, 32), blocks_per_row=6, runs=10):
     """The reference's default run (main.cpp:383-398 -> measure_diag_matrices,
     main.cpp:318-344): gen_n_diag_bcsr matrices (FP32 by default, 50 000 block
@@ -871,52 +936,8 @@ def run_ndiag(args, sizes=(2, 4, 8, 16, 32), blocks_per_row=6, runs=10):
     stream = torch.cuda.current_stream()
     for bs in sizes:
         rp, c, v = bm.gen_n_diag_bcsr(n_rows, blocks_per_row, bs, dt)
-        crp, cc, cv = bm.bcsr_to_csr(rp, c, v, bs)
-        vt = bm.transpose_blocks(rp, v, bs)
         x = np.ones(n_rows * bs, dtype=dt)  # main.cpp:27 sets x := 1
-        res = {}
-        y_ref = orc.csr_spmv(crp, cc, cv, x)
-        t0 = time.perf_counter()
-        for _ in range(runs):
-            orc.csr_spmv(crp, cc, cv, x)
-        res["CPU CSR"] = (time.perf_counter() - t0) / runs
-        d = {k: torch.from_numpy(a).cuda() for k, a in
-             (("rp", rp), ("c", c), ("v", v), ("vt", vt), ("crp", crp), ("cc", cc), ("cv", cv), ("x", x))}
-        dy = torch.empty(n_rows * bs, dtype=d["x"].dtype, device="cuda")
-        worst = 0.0
-        for var in range(bm.VARIANT_COUNT):
-            name = bm.variant_name(var)
-
-            def launch():
-                if bm.variant_is_csr(var):
-                    bm.csr_spmv(var, d["crp"], d["cc"], d["cv"], d["x"], dy)
-                else:
-                    vals = d["vt"] if bm.variant_layout(var) == 1 else d["v"]
-                    bm.bcsr_spmv(var, d["rp"], d["c"], vals, d["x"], dy, bs)
-            try:
-                launch()
-            except bm.BmfpError as e:
-                if e.status == bm.ERROR_NOT_SUPPORTED:
-                    continue  # e.g. the power-of-two variant at other bs, as gpu_matrix_multiplier.cu:1226
-                raise
-            torch.cuda.synchronize()
-            y = dy.cpu().numpy()
-            err = float(np.sum((y.astype(np.float64) - y_ref) ** 2) / np.sum(y_ref.astype(np.float64) ** 2))
-            worst = max(worst, err)
-            if err > 1e-9:
-                raise SystemExit(f"{name} bs {bs}: compare_results error {err:.3e}")
-            tot = 0.0
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            for _ in range(runs):
-                e0.record(stream)
-                launch()
-                e1.record(stream)
-                e1.synchronize()
-                tot += e0.elapsed_time(e1) * 1e-3
-            res[name] = tot / runs
-        results[str(bs)] = res
-        checks[str(bs)] = worst
-        del d, dy
+        results[str(bs)], checks[str(bs)] = measure_variants(rp, c, v, bs, x, runs, stream)
     if args.results_json:
         with open(args.results_json, "w") as f:
             json.dump(results, f, indent=2, sort_keys=True)
@@ -926,8 +947,49 @@ def run_ndiag(args, sizes=(2, 4, 8, 16, 32), blocks_per_row=6, runs=10):
                       "results": results, "fastest": best, "worst_compare_results": checks}), flush=True)
 
 
+def run_bridge(args, runs=10):
+    """The reference's bridge run (measure_golden_bridge, main.cpp:349-381, off
+    in its main): the Golden Gate truss of main.cpp:352-365 (128 km main span,
+    260 m towers, 7.62 m segments, FP64, bs 2) through every SpMV format, and
+    its solve as main.cpp:373-374 does it: Jacobi-preconditioned BiCGStab,
+    epsilon 0.8 on the recursive residual, 1000 iterations."""
+    import torch
+
+    import block_matrix_format_performance_gb300 as bm
+    from block_matrix_format_performance_gb300 import build as B
+    from oracle import oracle as orc
+    B.build()
+    orc.build()
+    t0 = time.perf_counter()
+    rp, c, v, rhs = bm.gen_golden_gate_bridge(args.bridge_main_span, 345.0, 260.0, 7.62, 450.0, -2e6)
+    gen_s = time.perf_counter() - t0
+    n = rp.size - 1
+    x = np.ones(2 * n)  # main.cpp:27 sets x := 1
+    res, worst = measure_variants(rp, c, v, 2, x, runs, torch.cuda.current_stream())
+    if args.results_json:
+        with open(args.results_json, "w") as f:
+            json.dump({"2": res}, f, indent=2, sort_keys=True)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    s = bm.Solver(A, "fp64", tol=0.8, max_iters=1000, preconditioner="jacobi", check_true_residual=False)
+    d_b = torch.from_numpy(rhs).cuda()
+    d_x = torch.empty_like(d_b)
+    s.solve(d_b, d_x)
+    info = s.solve(d_b, d_x)
+    s.close()
+    A.close()
+    best = min((k for k in res if k != "CPU CSR"), key=res.get)
+    print(json.dumps({"workload": "bridge", "main_span_m": args.bridge_main_span, "block_rows": n,
+                      "nnzb": int(c.size), "generate_s": round(gen_s, 3), "spmv_seconds": res, "fastest": best,
+                      "worst_compare_results": worst,
+                      "solve": {"epsilon": 0.8, "max_iterations": 1000, "preconditioner": "jacobi", **info}}),
+          flush=True)
+
+
 def main():
     args = parse_args()
+    if args.workload == "bridge":
+        run_bridge(args)
+        return
     if args.workload == "serve":
         run_serve(args)
         return

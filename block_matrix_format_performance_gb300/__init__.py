@@ -141,6 +141,26 @@ def gen_q4_elasticity(nx, ny, dtype=np.float64, young=1.0, poisson=0.3):
     return rp, c, v, rhs
 
 
+def gen_golden_gate_bridge(main_span=1280.0, side_span=345.0, tower_height=230.0, segment_length=7.62,
+                           load_window=450.0, load_fy=-2e6, dtype=np.float64):
+    """Truss model of the Golden Gate bridge (bmfp_gen_golden_gate_bridge): BCSR
+    bs=2 stiffness (row_ptr, cols, values) and load vector. main.cpp's bridge
+    is main_span=128000, tower_height=260."""
+    L = load()
+    e = dtype_enum(dtype)
+    args = (float(main_span), float(side_span), float(tower_height), float(segment_length), float(load_window),
+            float(load_fy))
+    nbr, nnzb = ctypes.c_int(0), ctypes.c_int64(0)
+    check(L.bmfp_gen_golden_gate_bridge(e, *args, ctypes.byref(nbr), ctypes.byref(nnzb), None, None, None, None))
+    rp = np.zeros(nbr.value + 1, np.int32)
+    c = np.zeros(nnzb.value, np.int32)
+    v = np.zeros(nnzb.value * 4, dtype)
+    rhs = np.zeros(2 * nbr.value, dtype)
+    check(L.bmfp_gen_golden_gate_bridge(e, *args, ctypes.byref(nbr), ctypes.byref(nnzb), _p(rp), _p(c), _p(v),
+                                        _p(rhs)))
+    return rp, c, v, rhs
+
+
 def bcsr_to_csr(row_ptr, cols, vals, bs):
     vals = np.ascontiguousarray(vals).reshape(-1)
     row_ptr = _i32(row_ptr)

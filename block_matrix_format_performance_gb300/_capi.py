@@ -64,6 +64,10 @@ SIGNATURES = {
     "bmfp_gen_band_bcsr": (c_int, [c_int, c_int, c_int, c_int, c_int, c_uint64, c_void_p, P(c_int64),
                                    c_void_p, c_void_p]),
     "bmfp_gen_uniform_vector": (c_int, [c_int, c_int64, c_uint64, c_uint64, c_void_p]),
+    "bmfp_gen_golden_gate_bridge": (c_int, [c_int, c_double, c_double, c_double, c_double, c_double, c_double,
+                                            P(c_int), P(c_int64), c_void_p, c_void_p, c_void_p, c_void_p]),
+    "bmfp_golden_gate_bridge_geometry": (c_int, [c_int, c_double, c_double, c_double, c_double, P(c_int), P(c_int),
+                                                 P(c_int), c_void_p, c_void_p, c_void_p, c_void_p]),
     "bmfp_gen_q4_elasticity": (c_int, [c_int, c_int, c_int, c_double, c_double, c_void_p, P(c_int64),
                                        c_void_p, c_void_p, c_void_p]),
     "bmfp_bcsr_spmv_bytes": (c_int64, [c_int, c_int, c_int, c_int, c_int64]),

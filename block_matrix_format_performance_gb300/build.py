@@ -38,6 +38,7 @@ SOURCES = [
     "serve.cpp",
     "cusparse.cpp",
     "host.cpp",
+    "bridge.cpp",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

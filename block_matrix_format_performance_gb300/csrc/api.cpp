@@ -444,6 +444,14 @@ int bmfp_matrix_set_lanes (bmfp_matrix_t m, int lanes, void *stream)
     return fail (BMFP_ERROR_INVALID_VALUE, "null matrix");
   if (lanes < 0 || (lanes > 32 && lanes != BMFP_LANES_ROW_OWNER && lanes != BMFP_LANES_COL_OWNER))
     return fail (BMFP_ERROR_INVALID_VALUE, "invalid lane count %d", lanes);
+  if (lanes != 0 && lanes != BMFP_LANES_COL_OWNER)
+    {
+      // only mappings this matrix's products can run (the autotuner's list)
+      int cand[12];
+      const int nc = native_lane_candidates (m->dtype, m->bs ? m->bs : 1, cand, 10);
+      if (std::find (cand, cand + nc, lanes) == cand + nc)
+        return fail (BMFP_ERROR_INVALID_VALUE, "lane count %d not valid for bs=%d", lanes, m->bs);
+    }
   return matrix_apply_lanes (m, lanes, as_stream (stream));
 }
 

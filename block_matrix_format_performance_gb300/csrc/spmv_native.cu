@@ -322,7 +322,13 @@ int native_default_lanes (int dtype, int bs, double avg_blocks_per_row)
     {
       switch (bs)
         {
-        case 2: return 4;
+        case 2:
+          // Two lanes own one scalar row each (no shuffle add); four lanes
+          // cover two blocks per step and tie only on rows of a multiple of
+          // eight blocks (the sweep's 8: 4 lanes picked; the bridge's 5
+          // blocks 18.2 vs 22.1 us, Q4 1000x250's 9 blocks 29.5 vs 32.6 us
+          // with 2 lanes).
+          return avg_blocks_per_row >= 7.5 && avg_blocks_per_row <= 8.5 ? 4 : 2;
         case 4: return 4;
         default: return BMFP_LANES_ROW_OWNER;
         }

@@ -481,6 +481,31 @@ BMFP_API int bmfp_gen_uniform_vector (int dtype, int64_t n, uint64_t seed, uint6
 BMFP_API int bmfp_gen_q4_elasticity (int dtype, int nx, int ny, double young, double poisson,
                                      int *row_ptr, int64_t *nnzb, int *cols, void *vals,
                                      void *rhs);
+/* Truss model of the Golden Gate bridge, fem_2d/golden_gate_bridge.h:101-237
+ * and :767-878 (golden_gate_bridge_2d<T, int, false>, the instantiation
+ * main.cpp:349-381 builds): BCSR bs=2 stiffness with one block row per node
+ * (supported DOFs left as zero rows and columns, as the reference leaves
+ * them) and the load vector (0, load_fy) on the deck's top chord within
+ * load_window of mid-span, else 0 (the load of main.cpp:356-363). main.cpp
+ * uses (main_span, side_span, tower_height, segment_length) = (128000, 345,
+ * 260, 7.62), window 450, fy -2e6. Pass 1 (row_ptr == NULL): *n_block_rows
+ * and *nnzb. Pass 2: row_ptr (n_block_rows+1), cols (nnzb), values
+ * (nnzb*4) and, if rhs != NULL, rhs (2*n_block_rows). Writes no files. */
+BMFP_API int bmfp_gen_golden_gate_bridge (int dtype, double main_span, double side_span,
+                                          double tower_height, double segment_length,
+                                          double load_window, double load_fy, int *n_block_rows,
+                                          int64_t *nnzb, int *row_ptr, int *cols, void *values,
+                                          void *rhs);
+/* Geometry of the same truss: *n_segments deck segments (top-chord nodes 4s
+ * and 4s+1 of segment s carry the loads, golden_gate_bridge.h:170-178),
+ * node coordinates xs/ys (*n_nodes each) and element end nodes starts/ends
+ * (*n_elements each, start < end). NULL arrays are skipped, so one call with
+ * all arrays NULL returns the sizes. For loads of any shape and for VTK
+ * output (golden_gate_bridge.h:239-282) through the C++ drop-in. */
+BMFP_API int bmfp_golden_gate_bridge_geometry (int dtype, double main_span, double side_span,
+                                               double tower_height, double segment_length,
+                                               int *n_segments, int *n_nodes, int *n_elements,
+                                               void *xs, void *ys, int *starts, int *ends);
 /* MatrixMarket coordinate file -> CSR (new; the reference only writes such
  * files, csr_matrix_class::write_mm, common/matrix_converters.h:119-144, with
  * common/mmio.c). Fields real, double, integer or pattern (1.0); symmetry

@@ -12,7 +12,8 @@
 //          (:32-49) and the BCSR->CSR constructor (:88-117).
 //   bridge prefix
 //          golden_gate_bridge_2d<double,int,false> on a short span: its BCSR
-//          stiffness matrix (golden_gate_bridge.h:767-878), forces_rhs and CSR.
+//          stiffness matrix (golden_gate_bridge.h:767-878), forces_rhs, CSR
+//          and write_vtk output (:239-282), plain and displaced.
 //   compare f32|f64 n file_a file_b
 //          compare_results (measurement_class.h:58-87); prints FLAGGED or OK.
 //   measure elapsed bytes ops [elapsed bytes ops ...]
@@ -105,6 +106,13 @@ static int run_bridge (const std::string &prefix)
   golden_gate_bridge_2d<double, int, false> bridge (load, main_len, side, 230.0, 7.62);
   dump_bcsr (prefix, *bridge.matrix);
   dump (prefix + ".rhs", bridge.forces_rhs.get (), (size_t) bridge.matrix->n_rows * 2);
+  // write_vtk (golden_gate_bridge.h:239-282), plain and with a fixed
+  // displacement pattern d_i = ((i mod 7) - 3) / 1000
+  bridge.write_vtk (prefix + ".vtk");
+  std::vector<double> disp ((size_t) bridge.matrix->n_rows * 2);
+  for (size_t i = 0; i < disp.size (); i++)
+    disp[i] = ((int) (i % 7) - 3) * 0.001;
+  bridge.write_vtk (prefix + "_disp.vtk", disp.data ());
   return 0;
 }
 

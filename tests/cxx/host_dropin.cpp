@@ -5,6 +5,8 @@
 //   host_dropin <out_dir> <f32|f64> <n_rows> <blocks_per_row> <bs>
 //   host_dropin <out_dir> mm
 //   host_dropin <out_dir> measure
+//   host_dropin <out_dir> bridge
+#include "golden_gate_bridge.h"
 #include "matrix_converters.h"
 #include "measurement_class.h"
 
@@ -62,6 +64,30 @@ int main (int argc, char **argv)
       total.finalize ();
       std::printf ("%.17g %.17g %.17g %s\n", total.get_elapsed (), total.get_effective_bandwidth (),
                    total.get_computational_throughput (), total.get_format ().c_str ());
+      return 0;
+    }
+  if (mode == "bridge")
+    {
+      // the fixture's bridge: a 1280 m main span, 345 m sides, 230 m towers,
+      // the load of main.cpp:356-363
+      const double side = 345.0, main_len = 1280.0;
+      auto load = [=] (double x) -> std::pair<double, double> {
+        const double mid = (main_len + side * 2) / 2;
+        if (x > mid - 450 && x < mid + 450)
+          return { 0, -2000000.0 };
+        return { 0, 0 };
+      };
+      golden_gate_bridge_2d<double, int, false> bridge (load, main_len, side, 230.0, 7.62);
+      const auto &m = *bridge.matrix;
+      dump (dir + "/bcsr_row_ptr", m.row_ptr.get (), (size_t) m.n_rows + 1);
+      dump (dir + "/bcsr_cols", m.columns.get (), (size_t) m.nnzb);
+      dump (dir + "/bcsr_vals", m.values.get (), (size_t) m.size ());
+      dump (dir + "/rhs", bridge.forces_rhs.get (), (size_t) m.n_rows * 2);
+      bridge.write_vtk (dir + "/bridge.vtk");
+      std::vector<double> disp ((size_t) m.n_rows * 2);
+      for (size_t i = 0; i < disp.size (); i++)
+        disp[i] = ((int) (i % 7) - 3) * 0.001;
+      bridge.write_vtk (dir + "/bridge_disp.vtk", disp.data ());
       return 0;
     }
   if (argc != 6)

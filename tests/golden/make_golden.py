@@ -10,6 +10,9 @@ they are mounted) and packs its raw outputs into compressed ``.npz`` files:
   bridge_f64.npz
       golden_gate_bridge_2d<double,int,false> stiffness (BCSR bs=2), rhs, CSR
       (fem_2d/golden_gate_bridge.h:767-878)
+  bridge.vtk, bridge_disp.vtk
+      its write_vtk output, plain and with displacement ((i mod 7) - 3) / 1000
+      (fem_2d/golden_gate_bridge.h:239-282)
   compare_results.json
       which vector pairs compare_results flags (common/measurement_class.h:58-87)
   measurement.json
@@ -72,6 +75,9 @@ def main():
         case = read_case(prefix, "f64")
         case["rhs"] = np.fromfile(prefix + ".rhs", dtype=np.float64)
         np.savez_compressed(os.path.join(HERE, "bridge_f64.npz"), **case)
+        for suffix in (".vtk", "_disp.vtk"):
+            with open(prefix + suffix) as src, open(os.path.join(HERE, "bridge" + suffix), "w") as dst:
+                dst.write(src.read())
 
         # compare_results around its 1e-9 threshold, both element types.
         rng = np.random.default_rng(7)

@@ -75,3 +75,14 @@ def test_stream_read_floor(cuda):
         bm.stream_read(buf, 24)
     with pytest.raises(bm.BmfpError):  # misaligned start
         bm.stream_read(buf[1:], 16)
+
+
+def test_bridge_workload_line(cuda, tmp_path):
+    out = tmp_path / "bridge.json"
+    line = run_bench("--workload", "bridge", "--bridge-main-span", "1280", "--results-json", str(out))
+    res = json.load(open(out))["2"]
+    for f in REFERENCE_FORMATS:
+        assert f in res, f
+    assert line["spmv_seconds"] == res and line["worst_compare_results"] <= 1e-9
+    assert line["block_rows"] > 1000 and line["solve"]["status"] == 0
+    assert line["solve"]["recursive_rel_residual"] < 0.8

@@ -79,6 +79,8 @@ def test_invalid_arguments_fail_without_touching_a_device(lib):
 
 def test_native_lane_heuristic(lib):
     assert bm.native_default_lanes(np.float64, 2, 8.0) == 4
+    assert bm.native_default_lanes(np.float64, 2, 5.0) == 2  # short rows: one lane per scalar row
+    assert bm.native_default_lanes(np.float64, 2, 9.0) == 2
     assert bm.native_default_lanes(np.float64, 32, 8.0) == 64  # one lane per scalar row
     assert bm.native_default_lanes(np.float32, 2, 8.0) == 2
     for bs in (2, 4, 8, 16, 32):

@@ -49,6 +49,19 @@ def test_write_mm_is_byte_identical(host_bin, tmp_path):
     assert open(tmp_path / "out.mtx").read() == open(os.path.join(GOLDEN, "ndiag_6x3_bs2.mtx")).read()
 
 
+def test_golden_gate_bridge_class_matches_reference(host_bin, tmp_path):
+    # golden_gate_bridge_2d<double, int, false> through the drop-in header:
+    # matrix, load vector and write_vtk output as the reference's own class
+    g = load_golden("bridge_f64.npz")
+    subprocess.run([host_bin, str(tmp_path), "bridge"], check=True, capture_output=True)
+    for field, ref in (("bcsr_row_ptr", g["bcsr_row_ptr"]), ("bcsr_cols", g["bcsr_cols"]),
+                       ("bcsr_vals", g["bcsr_vals"]), ("rhs", g["rhs"])):
+        got = np.fromfile(tmp_path / field, dtype=ref.dtype)
+        assert np.array_equal(got.view(np.uint8), np.ascontiguousarray(ref).view(np.uint8)), field
+    for name in ("bridge.vtk", "bridge_disp.vtk"):
+        assert open(tmp_path / name).read() == open(os.path.join(GOLDEN, name)).read(), name
+
+
 def test_measurement_class_matches_reference(host_bin, tmp_path):
     import json
     ref = json.load(open(os.path.join(GOLDEN, "measurement.json")))[0]

@@ -299,6 +299,19 @@ def test_column_owner_rejected_where_it_does_not_apply(lib, cuda):
     m.close()
 
 
+def test_lane_choices_the_matrix_cannot_run_are_refused(lib, cuda):
+    rp, c, v = ragged_bcsr(100, 100, 2, seed=3, dtype=np.float64)
+    m = bm.Matrix.from_bcsr(rp, c, v, 2)
+    for bad in (bm.LANES_ROW_OWNER, 3, 64 + 7):  # row owner needs bs >= 4; lanes are powers of two
+        with pytest.raises(bm.BmfpError):
+            m.set_lanes(bad)
+    m.set_lanes(2)
+    x = dev(np.ones(200))
+    y = dev(np.zeros(200))
+    m.spmv(x, y)
+    m.close()
+
+
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 @pytest.mark.parametrize("bs", [4, 8, 16, 32])
 def test_column_owner_on_caller_arrays(lib, orc, cuda, bs, dtype):
