@@ -854,7 +854,9 @@ def measure_variants(rp, c, v, bs, x, runs, stream):
     main.cpp:131-148): "CPU CSR" is the single-thread CPU loop (main.cpp:21-63)
     through the oracle's restatement; each GPU format is checked against it
     with compare_results' rule (sum (a-b)^2 / sum b^2 <= 1e-9,
-    measurement_class.h:58-87) and timed `runs` times between CUDA events.
+    measurement_class.h:58-87) and timed over `runs` back-to-back launches
+    between CUDA events (the reference records events around each launch;
+    here that would add the host's launch latency to every run).
     Returns ({format: mean seconds}, worst compare_results error)."""
     import torch
 
@@ -899,15 +901,16 @@ def measure_variants(rp, c, v, bs, x, runs, stream):
         worst = max(worst, err)
         if err > 1e-9:
             raise SystemExit(f"{name} bs {bs}: compare_results error {err:.3e}")
-        tot = 0.0
+        # `runs` launches back to back between one pair of events: the mean
+        # kernel time without the host's launch latency between runs (a few
+        # microseconds through Python, as long as a product of these sizes)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
         for _ in range(runs):
-            e0.record(stream)
             launch()
-            e1.record(stream)
-            e1.synchronize()
-            tot += e0.elapsed_time(e1) * 1e-3
-        res[name] = tot / runs
+        e1.record(stream)
+        e1.synchronize()
+        res[name] = e0.elapsed_time(e1) * 1e-3 / runs
     return res, worst
 
 
@@ -916,7 +919,7 @@ def run_ndiag(args, sizes=(2, 4, 8, 16, 32), blocks_per_row=6, runs=10):
     main.cpp:318-344): gen_n_diag_bcsr matrices (FP32 by default, 50 000 block
     rows, 6 blocks per row) for bs 2..32, every format timed `runs` times and
     averaged (perform_measurements, main.cpp:131-148), kernels only between
-    CUDA events as gpu_matrix_multiplier.cu times them. The output map
+    CUDA events (see measure_variants). The output map
     {bs: {format: mean seconds}} is the layout of the reference's
     results/result.json, which its plot/plot.py reads; "CPU CSR" is the
     single-thread CPU loop (main.cpp:21-63), timed through the oracle's
