@@ -854,9 +854,10 @@ def measure_variants(rp, c, v, bs, x, runs, stream):
     main.cpp:131-148): "CPU CSR" is the single-thread CPU loop (main.cpp:21-63)
     through the oracle's restatement; each GPU format is checked against it
     with compare_results' rule (sum (a-b)^2 / sum b^2 <= 1e-9,
-    measurement_class.h:58-87) and timed over `runs` back-to-back launches
-    between CUDA events (the reference records events around each launch;
-    here that would add the host's launch latency to every run).
+    measurement_class.h:58-87) and timed over `runs` launches replayed from a
+    CUDA graph between CUDA events (replay_seconds; the reference records
+    events around each launch, which here would time the host's launch
+    latency).
     Returns ({format: mean seconds}, worst compare_results error)."""
     import torch
 
@@ -901,17 +902,38 @@ def measure_variants(rp, c, v, bs, x, runs, stream):
         worst = max(worst, err)
         if err > 1e-9:
             raise SystemExit(f"{name} bs {bs}: compare_results error {err:.3e}")
-        # `runs` launches back to back between one pair of events: the mean
-        # kernel time without the host's launch latency between runs (a few
-        # microseconds through Python, as long as a product of these sizes)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
+        res[name] = replay_seconds(launch, runs, stream)
+    return res, worst
+
+
+def replay_seconds(launch, runs, stream):
+    """Mean device time of one launch: `runs` launches captured in a CUDA graph
+    and replayed between one pair of events, so the host's launch latency
+    (10 us and more through Python, longer than a small product) does not
+    sit between them. Launch sequences that cannot be captured are timed
+    back to back instead."""
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    graph = None
+    try:
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            for _ in range(runs):
+                launch()
+        g.replay()
+        torch.cuda.synchronize()
+        graph = g
+    except Exception:
+        torch.cuda.synchronize()
+    e0.record(stream)
+    if graph is not None:
+        graph.replay()
+    else:
         for _ in range(runs):
             launch()
-        e1.record(stream)
-        e1.synchronize()
-        res[name] = e0.elapsed_time(e1) * 1e-3 / runs
-    return res, worst
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) * 1e-3 / runs
 
 
 def run_ndiag(args, sizes=(2, 4, 8, 16, 32), blocks_per_row=6, runs=10):
