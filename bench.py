@@ -875,7 +875,7 @@ def measure_variants(rp, c, v, bs, x, runs, stream):
     d = {k: torch.from_numpy(a).cuda() for k, a in
          (("rp", rp), ("c", c), ("v", v), ("vt", vt), ("crp", crp), ("cc", cc), ("cv", cv), ("x", x))}
     dy = torch.empty(n, dtype=d["x"].dtype, device="cuda")
-    colown = v.dtype == np.float64 and bs in (4, 8, 16, 32)
+    colown = v.dtype == np.float64 and bs in (2, 4, 8, 16, 32)
     worst = 0.0
     for var in range(bm.VARIANT_COUNT):
         name = bm.variant_name(var)

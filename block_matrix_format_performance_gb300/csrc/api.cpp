@@ -399,7 +399,7 @@ int bmfp_matrix_device_arrays (bmfp_matrix_t m, const int **d_row_ptr, const int
   return BMFP_SUCCESS;
 }
 
-static bool col_owner_bs (int bs) { return bs == 4 || bs == 8 || bs == 16 || bs == 32; }
+static bool col_owner_bs (int bs) { return bs == 2 || bs == 4 || bs == 8 || bs == 16 || bs == 32; }
 
 // Builds (or, for any other mapping, releases) the column-major copy the
 // column-owner kernel reads.
@@ -408,7 +408,7 @@ static int matrix_apply_lanes (bmfp_matrix_s *m, int lanes, cudaStream_t s)
   if (lanes == BMFP_LANES_COL_OWNER)
     {
       if (m->bs == 0 || !col_owner_bs (m->bs))
-        return fail (BMFP_ERROR_INVALID_VALUE, "column-owner mapping needs a BCSR handle with bs in {4,8,16,32}");
+        return fail (BMFP_ERROR_INVALID_VALUE, "column-owner mapping needs a BCSR handle with bs in {2,4,8,16,32}");
       if (!m->d_vals_cm)
         {
           const size_t bytes = dtype_size (m->dtype) * (size_t) std::max<int64_t> (m->nnz * m->bs * m->bs, 1);

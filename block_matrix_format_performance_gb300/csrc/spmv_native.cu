@@ -379,8 +379,8 @@ int spmv_native_bcsr_colmajor (int dtype, int nbr, int bs, const int *rp, const 
 {
   if (nbr == 0)
     return BMFP_SUCCESS;
-  if (!(bs == 4 || bs == 8 || bs == 16 || bs == 32))
-    return fail (BMFP_ERROR_INVALID_VALUE, "column-owner mapping needs bs in {4,8,16,32}");
+  if (!(bs == 2 || bs == 4 || bs == 8 || bs == 16 || bs == 32))
+    return fail (BMFP_ERROR_INVALID_VALUE, "column-owner mapping needs bs in {2,4,8,16,32}");
   const int64_t threads = (int64_t) nbr * bs;
   const unsigned grid = (unsigned) ((threads + kThreads - 1) / kThreads);
 #define BMFP_COL(T, B)                                                                                              \
@@ -390,12 +390,12 @@ int spmv_native_bcsr_colmajor (int dtype, int nbr, int bs, const int *rp, const 
   if (dtype == BMFP_R64F)
     switch (bs)
       {
-        BMFP_COL (double, 4) BMFP_COL (double, 8) BMFP_COL (double, 16) BMFP_COL (double, 32)
+        BMFP_COL (double, 2) BMFP_COL (double, 4) BMFP_COL (double, 8) BMFP_COL (double, 16) BMFP_COL (double, 32)
       }
   else
     switch (bs)
       {
-        BMFP_COL (float, 4) BMFP_COL (float, 8) BMFP_COL (float, 16) BMFP_COL (float, 32)
+        BMFP_COL (float, 2) BMFP_COL (float, 4) BMFP_COL (float, 8) BMFP_COL (float, 16) BMFP_COL (float, 32)
       }
 #undef BMFP_COL
   BMFP_LAUNCH_CHECK ();

@@ -155,7 +155,7 @@ BMFP_API int bmfp_bcsr_spmv (int dtype, int variant, int n_block_rows, int n_blo
  * per scalar row over a column-major copy of the blocks that the handle then
  * keeps, so the lanes of a block read one contiguous column per load. The
  * fastest FP64 mapping from bs 16 on (GB300's FP64 pipe busy most of the
- * time); costs a second copy of the values in HBM. bs in {4,8,16,32}. */
+ * time); costs a second copy of the values in HBM. bs in {2,4,8,16,32}. */
 #define BMFP_LANES_COL_OWNER 65
 BMFP_API int bmfp_bcsr_spmv_native_ex (int dtype, int n_block_rows, int bs, int64_t nnzb,
                                        const int *d_row_ptr, const int *d_cols,
@@ -165,7 +165,8 @@ BMFP_API int bmfp_bcsr_native_default_lanes (int dtype, int bs, double avg_block
 /* The column-owner product (BMFP_LANES_COL_OWNER) on caller arrays whose
  * blocks are already column-major (the transpose_blocks layout the
  * reference's column-major variants take, gpu/gpu_matrix_multiplier.cu:
- * 341-400). bs in {4,8,16,32}. The fastest FP64 product from bs 8 on. */
+ * 341-400). bs in {2,4,8,16,32}. The fastest FP64 product from bs 8 on
+ * with the matrix coming from HBM, and at every bs while it stays in L2. */
 BMFP_API int bmfp_bcsr_spmv_colmajor (int dtype, int n_block_rows, int bs, int64_t nnzb,
                                       const int *d_row_ptr, const int *d_cols,
                                       const void *d_values_colmajor, const void *d_x, void *d_y,

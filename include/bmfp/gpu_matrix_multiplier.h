@@ -145,9 +145,9 @@ std::vector<measurement_class> gpu_bcsr_spmv (bcsr_matrix_class<data_type, index
     {
       const data_type *vals = bmfp_spmv_variant_layout (variant) == 1 ? col_major.ptr : row_major.ptr;
       // The native entry takes the column owner on the transposed blocks the
-      // caller passes where that is the faster product (FP64, bs 4..32).
+      // caller passes where that is the faster product (FP64, bs 2..32).
       const bool col_owner = variant == BMFP_SPMV_BCSR_NATIVE && sizeof (data_type) == 8
-                             && (bs == 4 || bs == 8 || bs == 16 || bs == 32);
+                             && (bs == 2 || bs == 4 || bs == 8 || bs == 16 || bs == 32);
       cuda_throw (cudaMemset (y.ptr, 0, sizeof (data_type) * ny), "cudaMemset");
       bool ok = false;
       const double elapsed = time_launch (

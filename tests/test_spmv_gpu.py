@@ -263,7 +263,7 @@ def test_host_buffer_spmv_edges(lib, orc, cuda):
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
-@pytest.mark.parametrize("bs", [4, 8, 16, 32])
+@pytest.mark.parametrize("bs", [2, 4, 8, 16, 32])
 def test_column_owner_mapping(lib, orc, cuda, bs, dtype):
     """BMFP_LANES_COL_OWNER: the handle keeps a column-major copy of its blocks
     and one lane per scalar row walks its columns; same parity bar as every
@@ -313,7 +313,7 @@ def test_lane_choices_the_matrix_cannot_run_are_refused(lib, cuda):
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
-@pytest.mark.parametrize("bs", [4, 8, 16, 32])
+@pytest.mark.parametrize("bs", [2, 4, 8, 16, 32])
 def test_column_owner_on_caller_arrays(lib, orc, cuda, bs, dtype):
     """bmfp_bcsr_spmv_colmajor on the transpose_blocks layout the caller holds."""
     import torch
