@@ -509,8 +509,10 @@ def run_ours(args):
                      "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                      else "fallback 6.8 TB/s", "unit": "GB/s", "frac": round(achieved / hbm, 4),
                      "traffic": traffic, "algorithmic_bytes": dcs["bytes"], "fp64_pipe": fp64_bound},
-        "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "s_per_step": round(e2e_s, 4)},
+        # not measured (--e2e-steps 0): null rather than NaN, which is not JSON
+        "e2e": {"value": round(e2e_value, 2) if e2e_value == e2e_value else None, "unit": "GB/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "s_per_step": round(e2e_s, 4) if e2e_s == e2e_s else None},
         "gpu_launches": args.steps * n,
         "clocks": clocks.summary(),
     }
