@@ -38,6 +38,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import re
 import statistics
@@ -125,6 +126,20 @@ def np_dt(tag):
 def case_bytes(bs, tag, nnzb, nbr=NBR):
     S = 8 if tag == "f64" else 4
     return nnzb * bs * bs * S + nnzb * 4 + (nbr + 1) * 4 + 2 * nbr * bs * S
+
+
+def json_line(obj):
+    """One strict JSON line: non-finite floats (a quantity not measured or not
+    evaluated) become null, since NaN and Infinity are not JSON."""
+    def clean(o):
+        if isinstance(o, float) and not math.isfinite(o):
+            return None
+        if isinstance(o, dict):
+            return {k: clean(v) for k, v in o.items()}
+        if isinstance(o, (list, tuple)):
+            return [clean(v) for v in o]
+        return o
+    return json.dumps(clean(obj), allow_nan=False)
 
 
 def max_over_ranks(value, dist, device):
@@ -524,7 +539,7 @@ def run_ours(args):
         line["solves_implicit_step"] = {"workload": "the same 256 grids with K + 1e-3 I (implicit time step, unit "
                                                     "lumped mass): FP32 inner solves converge", **solves_shifted}
     if rank == 0:
-        print(json.dumps(line), flush=True)
+        print(json_line(line), flush=True)
     if dist:
         dist.destroy_process_group()
 
@@ -604,7 +619,7 @@ def run_reference(args):
                                    "cuda_jit submodules, so it is not built)"},
         "e2e": {"value": round(value, 2), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    print(json.dumps(line), flush=True)
+    print(json_line(line), flush=True)
 
 
 def run_solve(args):
@@ -648,7 +663,7 @@ def run_solve(args):
         line.update(out)
         ref = xs["fp64"].double()
         line["mixed_error_vs_fp64"] = float(torch.linalg.norm(xs["mixed"].double() - ref) / torch.linalg.norm(ref))
-    print(json.dumps(line), flush=True)
+    print(json_line(line), flush=True)
     A.close()
 
 
@@ -734,7 +749,7 @@ def run_batch(args):
     shift = args.shift if args.matrix == "shifted" else None
     res = measure_batch([args.precision], args.tol, args.max_iters, args.repeats, args.systems,
                         per_request=args.repeats > 0, grid=grid, shift=shift)
-    print(json.dumps({"workload": "batch", "precision": args.precision,
+    print(json_line({"workload": "batch", "precision": args.precision,
                       "matrix": "q4" if shift is None else f"q4+{shift:g}I", **res}), flush=True)
 
 
@@ -838,7 +853,7 @@ def run_serve(args):
         "latency_p99_s": round(float(np.percentile(base_lat, 99)), 4)}
     bad = [{"grid": list(grids[k]), "status": i["status"], "true_rel": i["true_rel_residual"]}
            for k, i in enumerate(infos) if i["status"] != 0][:12]
-    print(json.dumps({
+    print(json_line({
         "workload": "serve", "matrix": "q4" if args.matrix == "q4" else f"q4+{args.shift:g}I",
         "requests": len(grids), "rate_req_s": args.rate, "precision": args.precision,
         "tol": args.tol, "large_requests": int(sum(g == (1000, 250) for g in grids)),
@@ -969,7 +984,7 @@ def run_ndiag(args, sizes=(2, 4, 8, 16, 32), blocks_per_row=6, runs=10):
         with open(args.results_json, "w") as f:
             json.dump(results, f, indent=2, sort_keys=True)
     best = {bs: min((k for k in r if k != "CPU CSR"), key=r.get) for bs, r in results.items()}
-    print(json.dumps({"workload": f"ndiag {args.ndiag_dtype}: gen_n_diag_bcsr {n_rows} block rows x "
+    print(json_line({"workload": f"ndiag {args.ndiag_dtype}: gen_n_diag_bcsr {n_rows} block rows x "
                                   f"{blocks_per_row} blocks, bs {list(sizes)}, {runs} runs per format",
                       "results": results, "fastest": best, "worst_compare_results": checks}), flush=True)
 
@@ -1007,7 +1022,7 @@ def run_bridge(args, runs=10):
     best = min((k for k in res if k != "CPU CSR"), key=res.get)
     # the reference's stop rule leaves the true residual unevaluated (NaN): null in JSON
     info = {k: (None if isinstance(v, float) and v != v else v) for k, v in info.items()}
-    print(json.dumps({"workload": "bridge", "main_span_m": args.bridge_main_span, "block_rows": n,
+    print(json_line({"workload": "bridge", "main_span_m": args.bridge_main_span, "block_rows": n,
                       "nnzb": int(c.size), "generate_s": round(gen_s, 3), "spmv_seconds": res, "fastest": best,
                       "worst_compare_results": worst,
                       "solve": {"epsilon": 0.8, "max_iterations": 1000, "preconditioner": "jacobi", **info}}),

@@ -9,12 +9,16 @@ import sys
 from conftest import ROOT
 
 
+def _no_nan(token):
+    raise ValueError(f"{token} in the JSON line")
+
+
 def test_reference_arm_line(lib, orc):
     p = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
                         "--warmup", "1", "--sizes", "2,4", "--dtypes", "f64"],
                        capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert p.returncode == 0, p.stderr[-2000:]
-    line = json.loads(p.stdout.strip().splitlines()[-1])
+    line = json.loads(p.stdout.strip().splitlines()[-1], parse_constant=_no_nan)  # strict JSON
     assert line["impl"] == "reference" and line["unit"] == "GB/s" and line["value"] > 0
     assert line["higher_is_better"] is True and line["n_gpus"] == 1
     cb = line["cpu_baseline"]

@@ -28,7 +28,11 @@ def run_bench(*argv, timeout=900):
     p = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), *argv], capture_output=True, text=True,
                        timeout=timeout, cwd=ROOT)
     assert p.returncode == 0, p.stderr[-3000:]
-    return json.loads(p.stdout.strip().splitlines()[-1])
+    return json.loads(p.stdout.strip().splitlines()[-1], parse_constant=_no_nan)  # strict JSON
+
+
+def _no_nan(token):
+    raise ValueError(f"{token} in the JSON line")
 
 
 def test_ndiag_writes_reference_result_json(cuda, tmp_path):
