@@ -77,3 +77,30 @@ def test_bridge_solve_as_main_cpp_does(lib, orc, cuda):
     K = sp.csr_matrix((cv, cc, crp))
     rel = np.linalg.norm(rhs - K @ x) / np.linalg.norm(rhs)
     assert abs(rel - info["recursive_rel_residual"]) <= 1e-6 * rel
+
+
+def test_bridge_geometry_matches_the_matrix(lib):
+    # bmfp_golden_gate_bridge_geometry: the nodes and bars behind the matrix
+    import ctypes
+    L = bm.load()
+    args = (bm.R64F, 1280.0, 345.0, 230.0, 7.62)
+    seg, nn, ne = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    assert L.bmfp_golden_gate_bridge_geometry(*args, ctypes.byref(seg), ctypes.byref(nn), ctypes.byref(ne),
+                                              None, None, None, None) == 0
+    xs, ys = np.zeros(nn.value), np.zeros(nn.value)
+    st, en = np.zeros(ne.value, np.int32), np.zeros(ne.value, np.int32)
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    assert L.bmfp_golden_gate_bridge_geometry(*args, ctypes.byref(seg), ctypes.byref(nn), ctypes.byref(ne),
+                                              p(xs), p(ys), p(st), p(en)) == 0
+    rp, c, v, rhs = bm.gen_golden_gate_bridge()
+    assert nn.value == rp.size - 1 and c.size == nn.value + 2 * ne.value
+    assert np.all(st < en) and en.max() < nn.value
+    # every bar is a pair of off-diagonal blocks in the pattern
+    for a, b in zip(st[::37], en[::37]):
+        assert b in c[rp[a]:rp[a + 1]] and a in c[rp[b]:rp[b + 1]]
+    # deck nodes 4s, 4s+1 lie on the top chord (78 m), the towers reach 230 m
+    assert np.all(ys[0:4 * seg.value:4] == 78.0) and ys.max() == 230.0
+    # loads sit on top-chord nodes inside the window around mid-span
+    loaded = np.nonzero(rhs)[0] // 2
+    mid = (1280.0 + 2 * 345.0) / 2
+    assert np.all(np.abs(xs[loaded] - mid) < 450.0) and np.all(loaded % 4 <= 1)
