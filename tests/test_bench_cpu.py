@@ -32,3 +32,11 @@ def test_reference_arm_only_rank0_prints(lib, orc):
                         "--warmup", "1", "--sizes", "2", "--dtypes", "f64"],
                        capture_output=True, text=True, timeout=600, cwd=ROOT, env=env)
     assert p.returncode == 0 and p.stdout.strip() == ""
+
+
+def test_json_lines_are_strict():
+    # a quantity not measured (NaN) or unbounded is written as null, never NaN
+    sys.path.insert(0, ROOT)
+    import bench
+    line = bench.json_line({"e2e": {"value": float("nan"), "s": float("inf")}, "v": [1.5, float("-inf")], "k": 2})
+    assert json.loads(line, parse_constant=_no_nan) == {"e2e": {"value": None, "s": None}, "v": [1.5, None], "k": 2}
