@@ -99,17 +99,19 @@ class SolverOptions(ctypes.Structure):
     _fields_ = [("precision", c_int), ("preconditioner", c_int), ("tolerance", c_double),
                 ("max_iterations", c_int), ("check_true_residual", c_int), ("inner_tolerance", c_double),
                 ("inner_max_iterations", c_int), ("max_refinements", c_int), ("fallback_fp64", c_int),
-                ("iterations_per_graph", c_int), ("ctas_per_sm", c_int), ("inner_stall_iterations", c_int)]
+                ("iterations_per_graph", c_int), ("ctas_per_sm", c_int), ("inner_stall_iterations", c_int),
+                ("residual_replacement", c_int)]
 
 
 class SolveInfo(ctypes.Structure):
     """struct bmfp_solve_info (include/bmfp.h)."""
     _fields_ = [("status", c_int), ("iterations", c_int), ("iterations_fp32", c_int), ("refinements", c_int),
                 ("restarts", c_int), ("used_fp64_fallback", c_int), ("true_rel_residual", c_double),
-                ("recursive_rel_residual", c_double), ("seconds", c_double)]
+                ("recursive_rel_residual", c_double), ("seconds", c_double), ("replacements", c_int),
+                ("pad", c_int)]
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_}
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "pad"}
 
 
 class ServerOptions(ctypes.Structure):

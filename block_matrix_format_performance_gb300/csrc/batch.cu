@@ -87,6 +87,46 @@ __device__ void team_sum (cg::cluster_group &cl, double (&v)[NK], double (&out)[
   cl.sync ();
 }
 
+// Team-wide maxima of NK non-negative values.
+template <int NK>
+__device__ void team_max (cg::cluster_group &cl, double (&v)[NK], double (&out)[NK])
+{
+  __shared__ double sh_w[NK][kMaxThreads / 32];
+  __shared__ double sh_cta[NK];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NK; k++)
+    {
+      double m = v[k];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1)
+        m = fmax (m, __shfl_xor_sync (0xffffffffu, m, off));
+      if (lane == 0)
+        sh_w[k][w] = m;
+    }
+  __syncthreads ();
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < NK; k++)
+      {
+        double a = 0.0;
+        for (int i = 0; i < nw; i++)
+          a = fmax (a, sh_w[k][i]);
+        sh_cta[k] = a;
+      }
+  cl.sync ();
+  const unsigned size = cl.num_blocks ();
+#pragma unroll
+  for (int k = 0; k < NK; k++)
+    {
+      double a = 0.0;
+      for (unsigned r = 0; r < size; r++)
+        a = fmax (a, *cl.map_shared_rank (&sh_cta[k], r));
+      out[k] = a;
+    }
+  cl.sync ();
+}
+
 template <typename T> struct TeamSys
 {
   int nbr, bs;
@@ -185,6 +225,48 @@ struct EpiResid
   }
 };
 
+// Residual replacement: r = b - A x with (rh, r) and (r, r).
+struct EpiReplaceT
+{
+  const double *b;
+  double *r;
+  const double *rh;
+  double rhr = 0.0, rr = 0.0;
+  __device__ void operator() (int64_t i, double y)
+  {
+    const double ri = b[i] - y;
+    r[i] = ri;
+    rhr = fma (rh[i], ri, rhr);
+    rr = fma (ri, ri, rr);
+  }
+};
+
+// cA = (entries per scalar row) * ||A||_inf of one system, over the team:
+// the residual-replacement bound of team_bicgstab.
+template <typename T>
+__device__ double team_matrix_bound (cg::cluster_group &cl, const TeamSys<T> &S)
+{
+  const TeamIdx ix = team_index<1> (cl);
+  double amax = 0.0, cmax = 0.0;
+  for (int64_t i = ix.elem0; i < S.n; i += ix.elem_stride)
+    {
+      const int br = (int) (i / S.bs), r = (int) (i % S.bs);
+      double sum = 0.0;
+      int count = 0;
+      for (int k = S.rp[br]; k < S.rp[br + 1]; k++)
+        {
+          for (int c = 0; c < S.bs; c++)
+            sum += fabs ((double) S.vals[(size_t) k * S.bs * S.bs + (size_t) r * S.bs + c]);
+          count += S.bs;
+        }
+      amax = fmax (amax, sum);
+      cmax = fmax (cmax, (double) count);
+    }
+  double in[2] = { amax, cmax }, out[2];
+  team_max<2> (cl, in, out);
+  return out[0] * out[1];
+}
+
 struct SolveOut
 {
   int iters = 0;
@@ -197,27 +279,37 @@ struct Scal
 {
   double a, b, c;
   int status;
+  int rep; // replace r by the true residual before the next iteration
 };
 
 // One BiCGStab solve by the team. r0 = rhs (x updated in place from x0 = 0
 // when zero_x, else from the given x with rhs its residual). Stops when
 // ||r|| < tol * norm_ref (norm_ref <= 0: ||rhs||).
 //
-// With snap (FP64 runs), x is copied there whenever the recursive residual
-// has fallen 4x below the last copy, and a run that ends above that point
-// (breakdown, iteration limit) returns it; a residual that grows 1e8-fold
-// over the best seen, or turns non-finite, ends the run as a breakdown. Each
-// thread copies and restores the elements it also updates, so the copies
-// need no barrier of their own.
+// With snap (FP64 runs), the iterate is copied there whenever the recursive
+// residual has fallen 4x below the last copy, and a run that ends above that
+// point (breakdown, iteration limit) returns it; a residual that grows
+// 1e16-fold over the best seen, or turns non-finite, ends the run as a
+// breakdown. Each thread copies and restores the elements it also updates,
+// so the copies need no barrier of their own.
 //
 // stall > 0 (inner solves of mixed precision): a run whose best recursive
 // residual has not halved within a window of `stall` iterations (counted
 // from the start or from the last halving) ends with status 4. The caller
 // keeps such a run only if it halved at least once, so the iterations of a
 // plateau would be spent on a result the next refinement step redoes.
-template <typename T, int OP>
+//
+// RR (FP64 runs): residual replacement with group update (van der Vorst and
+// Ye 2000), the rule of the whole-GPU engine (DevState in solver.h): x is the
+// group base, the updates accumulate in xp; when the deviation bound
+//   dev += eps (cA ||xp|| + ||r||)
+// crosses kReplaceThreshold * ||r||, xp is folded into x and r is replaced
+// by the true residual bt - A x (bt: the system's b). Applied at once, in the
+// iteration where the bound crosses.
+template <typename T, int OP, bool RR = false>
 __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, const T *rhs, T *x, bool zero_x,
-                                   double tol, int max_it, double norm_ref, T *snap = nullptr, int stall = 0)
+                                   double tol, int max_it, double norm_ref, T *snap = nullptr, int stall = 0,
+                                   const T *bt = nullptr, T *xp = nullptr, double cA = 0.0, int *reps = nullptr)
 {
   using Op = TeamOp<T, OP>;
   const TeamIdx ix = team_index<Op::G> (cl);
@@ -229,14 +321,19 @@ __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, c
       const T ri = rhs[i];
       if (zero_x)
         x[i] = 0;
+      if (RR)
+        xp[i] = 0;
       S.r[i] = ri;
       S.rh[i] = ri;
       S.p[i] = 0;
       S.v[i] = 0;
       rr0 = fma ((double) ri, (double) ri, rr0);
     }
-  double in1[1] = { rr0 }, out1[1];
-  team_sum<1> (cl, in1, out1);
+  double in1[2] = { rr0, 0.0 }, out1[2];
+  if (RR && !zero_x)
+    for (int64_t i = ix.elem0; i < S.n; i += ix.elem_stride)
+      in1[1] = fma ((double) x[i], (double) x[i], in1[1]);
+  team_sum<2> (cl, in1, out1);
   if (threadIdx.x == 0)
     sc.a = norm_ref > 0.0 ? norm_ref : sqrt (out1[0]);
   __syncthreads ();
@@ -247,6 +344,12 @@ __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, c
   double rho_prev = 1.0, alpha = 1.0, omega = 1.0;
   // Team-uniform (every thread holds the same rr), so no broadcast needed.
   double best_rr = rr, snap_rr = INFINITY;
+  // Replacement bound: kept by thread 0 only, which takes every scalar
+  // decision (nn = (x', x') of the last iteration, or the base's (g, g) at
+  // the start and after a replacement, when reset says so).
+  constexpr double eps = 0x1p-53;
+  double dev = 0.0, dev0 = 0.0, nr_prev = 0.0, nn = out1[1];
+  bool reset = true;
   for (;;)
     {
       if (rr < best_rr)
@@ -259,7 +362,7 @@ __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, c
       if (snap && rr < 0.25 * snap_rr)
         {
           for (int64_t i = ix.elem0; i < S.n; i += ix.elem_stride)
-            snap[i] = x[i];
+            snap[i] = RR ? x[i] + xp[i] : x[i];
           snap_rr = rr;
         }
       // convergence, limits and beta (gpu/bicgstab.cu:451, :512)
@@ -282,9 +385,25 @@ __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, c
               if (!isfinite (beta))
                 st = 3;
             }
+          int rep = 0;
+          if (RR && st == 0)
+            {
+              const double nr = sqrt (rr);
+              if (reset)
+                dev = dev0 = eps * (cA * sqrt (nn) + nr);
+              else
+                {
+                  const double dnew = dev + eps * (cA * sqrt (nn) + nr);
+                  rep = dev <= kReplaceThreshold * nr_prev && dnew > kReplaceThreshold * nr && dnew > 1.1 * dev0;
+                  dev = dnew;
+                }
+              nr_prev = nr;
+              reset = rep;
+            }
           sc.b = beta;
           sc.c = nb > 0.0 ? sqrt (rr) / nb : 0.0;
           sc.status = st;
+          sc.rep = rep;
         }
       __syncthreads ();
       if (sc.status)
@@ -293,6 +412,31 @@ __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, c
           o.rec_rel = sc.c;
           break;
         }
+      if constexpr (RR)
+        if (sc.rep)
+          {
+            // Group update, then r = b - A x: every thread folds its own
+            // elements; the product reads everyone's, after the barrier.
+            double gg = 0.0;
+            for (int64_t i = ix.elem0; i < S.n; i += ix.elem_stride)
+              {
+                const T gi = x[i] + xp[i];
+                x[i] = gi;
+                xp[i] = 0;
+                gg = fma ((double) gi, (double) gi, gg);
+              }
+            cl.sync ();
+            EpiReplaceT er{ bt, S.r, S.rh };
+            Op::run (S, ix, x, S.t, er);
+            double d4[3] = { er.rhr, er.rr, gg }, nr4[3];
+            team_sum<3> (cl, d4, nr4);
+            rho = nr4[0];
+            rr = nr4[1];
+            nn = nr4[2];
+            if (reps)
+              (*reps)++;
+            continue; // convergence is checked on the replaced residual
+          }
       const T tb = (T) sc.b, tw = (T) omega;
       for (int64_t i = ix.elem0; i < S.n; i += ix.elem_stride)
         S.p[i] = S.r[i] + tb * (S.p[i] - tw * S.v[i]);
@@ -337,28 +481,43 @@ __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, c
         }
       omega = sc.a;
       const T tw2 = (T) omega;
-      double rhr = 0.0, rrn = 0.0;
+      double rhr = 0.0, rrn = 0.0, xx = 0.0;
+      T *xu = RR ? xp : x; // the vector the iteration updates
       for (int64_t i = ix.elem0; i < S.n; i += ix.elem_stride)
         {
-          x[i] = x[i] + ta * S.p[i] + tw2 * S.s[i];
+          const T xn = xu[i] + ta * S.p[i] + tw2 * S.s[i];
+          xu[i] = xn;
           const T ri = S.s[i] - tw2 * S.t[i];
           S.r[i] = ri;
           rhr = fma ((double) S.rh[i], (double) ri, rhr);
           rrn = fma ((double) ri, (double) ri, rrn);
+          if (RR)
+            xx = fma ((double) xn, (double) xn, xx);
         }
-      double d3[2] = { rhr, rrn }, nx[2];
-      team_sum<2> (cl, d3, nx);
+      double d3[3] = { rhr, rrn, xx }, nx[3];
+      team_sum<3> (cl, d3, nx);
       rho_prev = rho;
       rho = nx[0];
       rr = nx[1];
+      nn = nx[2];
       o.iters++;
     }
   if (snap && o.status != 1 && snap_rr < INFINITY && !(rr <= snap_rr))
     {
       for (int64_t i = ix.elem0; i < S.n; i += ix.elem_stride)
-        x[i] = snap[i];
+        {
+          x[i] = snap[i];
+          if (RR)
+            xp[i] = 0;
+        }
       o.rec_rel = nb > 0.0 ? sqrt (snap_rr) / nb : 0.0;
     }
+  if (RR)
+    for (int64_t i = ix.elem0; i < S.n; i += ix.elem_stride)
+      {
+        x[i] = x[i] + xp[i];
+        xp[i] = 0;
+      }
   cl.sync (); // x, r complete before anyone reads them
   return o;
 }
@@ -380,30 +539,36 @@ __device__ void team_residual (cg::cluster_group &cl, const TeamSys<double> &S, 
 
 struct Fp64Result
 {
-  int iters = 0, status = 0, restarts = 0;
+  int iters = 0, status = 0, restarts = 0, replacements = 0;
   double rel = 0.0, rec = 0.0;
 };
 
 // FP64 BiCGStab with true-residual restarts: from x = 0 (first) or from the
 // current x with its residual in r64. Restarts continue while each one still
-// lowers the true residual (at most 8). Near FP64's attainable accuracy a restart
+// lowers the true residual (at most 8); each aims at half the true residual
+// it starts from (a restart asked only for the tolerance again, from just
+// above it, moves x by a hair and the true residual with it). Near FP64's attainable accuracy a restart
 // can leave x worse (asking the recursive residual for less than the
 // tolerance only makes that more likely), so the best iterate is kept (xb)
 // and restored.
 template <int OP>
 __device__ Fp64Result fp64_restarted (cg::cluster_group &cl, const TeamSys<double> &S64, const BatchDesc &D,
-                                      const BatchParams &P, bool first, int budget, double norm_b, double *r64)
+                                      const BatchParams &P, bool first, int budget, double norm_b, double *r64,
+                                      double cA)
 {
   __shared__ double sh_rel, sh_nb;
   const TeamIdx ix = team_index<1> (cl);
   double *xb = D.w64 + 7 * D.n;
   double *snap = D.w64 + 8 * D.n;
+  double *xp = D.w64 + 9 * D.n;
   Fp64Result f;
   double best = INFINITY;
+  double target = P.tol; // a restart aims at half the true residual it starts from
   for (;;)
     {
-      const SolveOut o = team_bicgstab<double, OP> (cl, S64, first ? D.b : r64, D.x, first, P.tol, budget - f.iters,
-                                                    norm_b, snap);
+      const SolveOut o = team_bicgstab<double, OP, true> (cl, S64, first ? D.b : r64, D.x, first, target,
+                                                          budget - f.iters, norm_b, snap, 0, D.b, xp, cA,
+                                                          &f.replacements);
       f.iters += o.iters;
       double rr, bb;
       team_residual<OP> (cl, S64, D.b, D.x, r64, rr, bb);
@@ -445,6 +610,7 @@ __device__ Fp64Result fp64_restarted (cg::cluster_group &cl, const TeamSys<doubl
       cl.sync ();
       first = false;
       f.restarts++;
+      target = fmin (P.tol, 0.5 * rel);
     }
   return f;
 }
@@ -456,9 +622,11 @@ __device__ void solve_system (cg::cluster_group &cl, const BatchDesc &D, const B
                        D.w64, D.w64 + D.n, D.w64 + 2 * D.n, D.w64 + 3 * D.n, D.w64 + 4 * D.n, D.w64 + 5 * D.n };
   const TeamIdx ix = team_index<1> (cl);
   __shared__ double sh_rel, sh_scale;
-  int iters64 = 0, iters32 = 0, refinements = 0, fallback = 0, status = 0, restarts = 0;
+  int iters64 = 0, iters32 = 0, refinements = 0, fallback = 0, status = 0, restarts = 0, replacements = 0;
   double rel = 0.0, rec = 0.0;
   double *r64 = D.w64 + 6 * D.n; // FP64 residual of the refinement / restart loop
+  // Replacement bound of the FP64 runs (one pass over the matrix).
+  const double cA = PREC == BMFP_SOLVE_FP32 ? 0.0 : team_matrix_bound<double> (cl, S64);
   if constexpr (PREC == BMFP_SOLVE_FP32)
     {
       TeamSys<float> S32{ D.nbr, D.bs, D.n, D.rp, D.cols, D.vals32,
@@ -480,10 +648,11 @@ __device__ void solve_system (cg::cluster_group &cl, const BatchDesc &D, const B
     }
   else if constexpr (PREC == BMFP_SOLVE_FP64)
     {
-      const Fp64Result f = fp64_restarted<OP> (cl, S64, D, P, true, P.max_it, -1.0, r64);
+      const Fp64Result f = fp64_restarted<OP> (cl, S64, D, P, true, P.max_it, -1.0, r64, cA);
       iters64 = f.iters;
       status = f.status;
       restarts = f.restarts;
+      replacements = f.replacements;
       rel = f.rel;
       rec = f.rec;
     }
@@ -533,10 +702,11 @@ __device__ void solve_system (cg::cluster_group &cl, const BatchDesc &D, const B
               // exactly as the FP64 solve does (same ||b||, same bits).
               const bool fresh = rel > 1e-2;
               const Fp64Result f
-                = fp64_restarted<OP> (cl, S64, D, P, fresh, P.max_it - iters32, fresh ? -1.0 : nb, r64);
+                = fp64_restarted<OP> (cl, S64, D, P, fresh, P.max_it - iters32, fresh ? -1.0 : nb, r64, cA);
               iters64 += f.iters;
               status = f.status;
               restarts = f.restarts;
+              replacements = f.replacements;
               rel = f.rel;
               rec = f.rec;
               break;
@@ -581,6 +751,7 @@ __device__ void solve_system (cg::cluster_group &cl, const BatchDesc &D, const B
       res.iterations_fp32 = iters32;
       res.refinements = refinements;
       res.restarts = restarts;
+      res.replacements = replacements;
       res.fallback = fallback;
       res.true_rel = rel;
       res.rec_rel = rec;
@@ -715,7 +886,7 @@ int BatchEngine::init (int n, const bmfp_matrix_s *const *mats, const bmfp_solve
       total += rows[i];
     }
   const bool lowp = o.precision != BMFP_SOLVE_FP64;
-  BMFP_CUDA (cudaMalloc (&w64_, sizeof (double) * (size_t) std::max<int64_t> (9 * total, 1)));
+  BMFP_CUDA (cudaMalloc (&w64_, sizeof (double) * (size_t) std::max<int64_t> (kBatchW64 * total, 1)));
   if (lowp)
     BMFP_CUDA (cudaMalloc (&w32_, sizeof (float) * (size_t) std::max<int64_t> (8 * total, 1)));
   BMFP_CUDA (cudaMallocHost (&h_desc_, sizeof (BatchDesc) * (size_t) std::max (n, 1)));
@@ -745,7 +916,7 @@ int BatchEngine::init (int n, const bmfp_matrix_s *const *mats, const bmfp_solve
         op_ = D.op;
       else if (op_ != D.op)
         op_ = kOpTpr; // mixed block sizes: the generic warp-per-block-row routine
-      D.w64 = (double *) w64_ + 9 * off;
+      D.w64 = (double *) w64_ + kBatchW64 * off;
       D.w32 = lowp ? (float *) w32_ + 8 * off : nullptr;
       D.vals32 = nullptr;
       if (lowp)
@@ -892,6 +1063,7 @@ int BatchEngine::solve (const void *const *d_b, void *const *d_x, bmfp_solve_inf
       f.iterations_fp32 = o.iterations_fp32;
       f.refinements = o.refinements;
       f.restarts = o.restarts;
+      f.replacements = o.replacements;
       f.used_fp64_fallback = o.fallback;
       f.true_rel_residual = o.true_rel;
       f.recursive_rel_residual = o.rec_rel;

@@ -7,6 +7,9 @@
 
 namespace bmfp
 {
+// FP64 work vectors per system (BatchDesc::w64).
+constexpr int kBatchW64 = 10;
+
 // One system as the persistent kernel sees it.
 struct BatchDesc
 {
@@ -17,7 +20,7 @@ struct BatchDesc
   const float *vals32 = nullptr;
   const double *b = nullptr;
   double *x = nullptr;
-  double *w64 = nullptr; // 9 n: r, rh, p, v, s, t, residual, best x, in-run snapshot
+  double *w64 = nullptr; // kBatchW64 n: r, rh, p, v, s, t, residual, best x, in-run snapshot, x'
   float *w32 = nullptr;  // 8 n: r, rh, p, v, s, t, x32, rhs32
   double *x_out = nullptr; // optional copy of x as each system finishes (mapped host memory)
 };
@@ -31,7 +34,7 @@ struct BatchOut
   int iterations = 0, iterations_fp32 = 0, refinements = 0, restarts = 0, fallback = 0;
   double true_rel = 0.0, rec_rel = 0.0;
   int done = 0;
-  int pad = 0;
+  int replacements = 0;
 };
 
 struct BatchParams

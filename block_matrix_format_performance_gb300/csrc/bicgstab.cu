@@ -13,8 +13,8 @@
 //   phase 2  v = A q, partial (rh, v)       fused into the SpMV epilogue
 //   phase 3  alpha = rho / (rh, v);         s = r - alpha v;  z = P s
 //   phase 4  t = A z, partials (t, s), (t, t)
-//   phase 5  omega = (t, s) / (t, t);       x += alpha q + omega z;  r = s - omega t
-//            partials (rh, r), (r, r)
+//   phase 5  omega = (t, s) / (t, t);       x' += alpha q + omega z;  r = s - omega t
+//            partials (rh, r), (r, r), (x', x')
 //
 // Algorithmic traffic per iteration: 2 SpMV + 17 n vector elements (no
 // preconditioner). Dot products are per-CTA partial sums written by one phase
@@ -23,15 +23,25 @@
 // The host launches CUDA graphs of `chunk` iterations and only polls the
 // done flag between graphs; phases after convergence return immediately.
 //
+// Residual replacement with group update (van der Vorst and Ye 2000, see
+// DevState): phase 1 tracks the deviation bound and, when it is time,
+// replaces the p update of that iteration by the fold g += x', x' = 0; phase 2
+// of the same iteration then computes r = c - A g instead of v = A q (and
+// (rh, r), (r, r)), phases 3 and 4 return at once and phase 5 only marks the
+// replacement done. No kernel is added to the graph for it.
+//
 // Differences from the reference, on purpose: the solution returned is the
-// last iterate (the reference copied buffer half 0, bicgstab.cu:515), and a
-// solve finishes with a true-residual check b - A x (restarting from the true
-// residual when the recursive one has drifted below the tolerance first).
+// last iterate (the reference copied buffer half 0, bicgstab.cu:515), the
+// recursive residual is replaced by the true one near convergence (above),
+// and a solve finishes with a true-residual check b - A x (restarting from
+// the true residual when the recursive one has drifted below the tolerance
+// first).
 #include "solver.h"
 #include "spmv_core.cuh"
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 namespace bmfp
@@ -50,8 +60,12 @@ enum PartKind
   kTT = 4,
   kResRR = 5,
   kResBB = 6,
-  kParts = 7
+  kXX = 7, // (x', x') of phase 5
+  kGG = 8, // (g, g) after a fold (phase 1) or 0 at a run's start
+  kParts = 9
 };
+// The allocation-free entry point sizes its partial-sum slot by kRawParts.
+static_assert (kParts == kRawParts, "solver.h kRawParts must equal the number of partial kinds");
 
 template <typename T> struct Args
 {
@@ -61,6 +75,7 @@ template <typename T> struct Args
   int64_t n;
   T *x, *r, *rh, *p, *v, *q, *s, *z, *t;
   const T *P;
+  T *g, *xp; // group base and updates accumulated since the last replacement
   double *part;
   int grid;
   DevState *st;
@@ -212,12 +227,44 @@ template <typename T> struct EpiResidual
   }
 };
 
-// phase 2: v = A q, partial (rh, v)
+// Residual replacement: r = c - A g, with (rh, r) and (r, r).
+template <typename T> struct EpiReplace
+{
+  const T *c;
+  T *r;
+  const T *rh;
+  T rhr = 0, rr = 0;
+  __device__ void operator() (int64_t i, T y)
+  {
+    const T ri = c[i] - y;
+    r[i] = ri;
+    rhr = fma (rh[i], ri, rhr);
+    rr = fma (ri, ri, rr);
+  }
+};
+
+__device__ __forceinline__ bool replacing (const DevState *st)
+{
+  // Written by phase 1 of this iteration, an earlier kernel.
+  return st->rep_now != 0;
+}
+
+// phase 2: v = A q, partial (rh, v); in a replacement iteration r = c - A g
+// with partials (rh, r), (r, r) instead (A g lands in t, free until phase 4).
 template <typename T, class Op>
 __global__ void __launch_bounds__ (kThreads) phase_v (Args<T> a)
 {
   if (is_done (a.st))
     return;
+  if (replacing (a.st))
+    {
+      EpiReplace<T> e{ static_cast<const T *> (a.st->c), a.r, a.rh };
+      Op::run (a, a.g, a.t, e);
+      double vals[2] = { (double) e.rhr, (double) e.rr };
+      const int ks[2] = { kRhR, kRR };
+      store_parts<2> (vals, a.part, a.grid, ks);
+      return;
+    }
   EpiDot<T> e{ a.rh };
   Op::run (a, a.q, a.v, e);
   double vals[1] = { (double) e.acc };
@@ -229,7 +276,7 @@ __global__ void __launch_bounds__ (kThreads) phase_v (Args<T> a)
 template <typename T, class Op>
 __global__ void __launch_bounds__ (kThreads) phase_t (Args<T> a)
 {
-  if (is_done (a.st))
+  if (is_done (a.st) || replacing (a.st))
     return;
   EpiTS<T> e{ a.s };
   Op::run (a, a.z, a.t, e);
@@ -252,26 +299,29 @@ __global__ void __launch_bounds__ (kThreads)
 
 // ------------------------------------------------------------ vector phases
 
-// Fresh start (ZERO: x = 0, r = b) or restart from a given true residual.
+// Start of a run solving A e = c from e = 0 (ZERO: a fresh solve; else a
+// restart whose c is the true residual of the current x). x itself is not
+// touched until the run ends.
 template <typename T, bool ZERO>
 __global__ void __launch_bounds__ (kThreads)
-  start_kernel (Args<T> a, const T *src, double tol, int max_iter, double norm_b, int iter0)
+  start_kernel (Args<T> a, const T *src, double tol, int max_iter, double norm_b, int iter0, double eps,
+                double cA)
 {
   double rr = 0.0;
   GRID_STRIDE (i, a.n)
   {
     const T ri = src[i];
-    if (ZERO)
-      a.x[i] = 0;
     a.r[i] = ri;
     a.rh[i] = ri;
     a.p[i] = 0;
     a.v[i] = 0;
+    a.g[i] = 0;
+    a.xp[i] = 0;
     rr = fma ((double) ri, (double) ri, rr);
   }
-  double vals[2] = { rr, rr };
-  const int ks[2] = { kRhR, kRR };
-  store_parts<2> (vals, a.part, a.grid, ks);
+  double vals[3] = { rr, rr, 0.0 };
+  const int ks[3] = { kRhR, kRR, kGG };
+  store_parts<3> (vals, a.part, a.grid, ks);
   if (blockIdx.x == 0 && threadIdx.x == 0)
     {
       DevState *st = a.st;
@@ -283,6 +333,13 @@ __global__ void __launch_bounds__ (kThreads)
       st->max_iter = max_iter;
       st->done = 0;
       st->status = kStateRunning;
+      st->eps = eps;
+      st->cA = cA;
+      st->c = src;
+      st->rep_now = 0;
+      st->rep_done = 1; // phase 1 sets the deviation bound from (g, g) = 0 and ||r0||
+      st->replacements = 0;
+      st->dslot = 0;
       if (ZERO)
         {
           st->iter = 0;
@@ -308,14 +365,17 @@ __global__ void __launch_bounds__ (kThreads) phase_p (Args<T> a)
   DevState *st = a.st;
   if (is_done (st))
     return;
-  double s[2];
-  const int ks[2] = { kRhR, kRR };
-  sum_parts<2> (a.part, a.grid, ks, s);
+  // After a replacement (or at a run's start) the third sum is (g, g), which
+  // resets the deviation bound; otherwise it is (x', x').
+  const bool after_rep = st->rep_done != 0;
+  double s[3];
+  const int ks[3] = { kRhR, kRR, after_rep ? kGG : kXX };
+  sum_parts<3> (a.part, a.grid, ks, s);
   __shared__ double sh_beta, sh_omega;
-  __shared__ int sh_status;
+  __shared__ int sh_status, sh_rep;
   if (threadIdx.x == 0)
     {
-      const double rho = s[0], rr = s[1];
+      const double rho = s[0], rr = s[1], nn = s[2];
       const double nb_state = st->norm_b;
       const double nb = nb_state < 0.0 ? sqrt (rr) : nb_state;
       const double omega = st->omega;
@@ -333,28 +393,74 @@ __global__ void __launch_bounds__ (kThreads) phase_p (Args<T> a)
           if (!isfinite (beta))
             status = kStateBreakdown;
         }
+      int rep = 0;
+      const double eps = st->eps;
+      const int rd = st->dslot, wr = rd ^ 1;
+      double dev = 0.0, dev0 = 0.0;
+      const double nr = sqrt (rr);
+      if (status == kStateRunning && eps > 0.0)
+        {
+          if (after_rep)
+            dev = dev0 = eps * (st->cA * sqrt (nn) + nr);
+          else
+            {
+              dev = st->dev[rd] + eps * (st->cA * sqrt (nn) + nr);
+              dev0 = st->dev0[rd];
+              rep = st->dev[rd] <= kReplaceThreshold * st->nr_prev[rd] && dev > kReplaceThreshold * nr
+                    && dev > 1.1 * dev0;
+            }
+        }
       if (blockIdx.x == 0)
         {
           st->rr = rr;
+          st->dev[wr] = dev;
+          st->dev0[wr] = dev0;
+          st->nr_prev[wr] = nr;
           if (status != kStateRunning)
             {
               st->status = status;
               *reinterpret_cast<volatile int *> (&st->done) = 1;
             }
+          else if (rep)
+            {
+              st->rep_now = 1;
+              st->replacements = st->replacements + 1;
+            }
           else
-            st->rho = rho;
+            {
+              st->rep_now = 0;
+              st->rho = rho;
+            }
         }
       sh_beta = beta;
       sh_omega = omega;
       sh_status = status;
+      sh_rep = rep;
     }
   __syncthreads ();
   if (sh_status != kStateRunning)
     return;
+  const int64_t stride = (int64_t) gridDim.x * blockDim.x;
+  if (sh_rep)
+    {
+      // Group update: fold the accumulated updates into the base, which
+      // phase 2 multiplies by A for the true residual.
+      double gg = 0.0;
+      GRID_STRIDE (i, a.n)
+      {
+        const T gi = a.g[i] + a.xp[i];
+        a.g[i] = gi;
+        a.xp[i] = 0;
+        gg = fma ((double) gi, (double) gi, gg);
+      }
+      double vals[1] = { gg };
+      const int kg[1] = { kGG };
+      store_parts<1> (vals, a.part, a.grid, kg);
+      return;
+    }
   const T tb = (T) sh_beta, tw = (T) sh_omega;
   // Four grid-stride elements per pass, loads first (the arrays may alias as
   // far as the compiler knows, so it would not hoist them itself).
-  const int64_t stride = (int64_t) gridDim.x * blockDim.x;
   int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
   for (; i + 3 * stride < a.n; i += 4 * stride)
     {
@@ -389,7 +495,7 @@ template <typename T, bool PRE>
 __global__ void __launch_bounds__ (kThreads) phase_s (Args<T> a)
 {
   DevState *st = a.st;
-  if (is_done (st))
+  if (is_done (st) || replacing (st))
     return;
   double s[1];
   const int ks[1] = { kRhV };
@@ -456,6 +562,16 @@ __global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
   DevState *st = a.st;
   if (is_done (st))
     return;
+  if (replacing (st))
+    {
+      // r, (rh, r) and (r, r) came from phase 2; nothing else moves.
+      if (blockIdx.x == 0 && threadIdx.x == 0)
+        {
+          st->rep_done = 1;
+          st->dslot = st->dslot ^ 1;
+        }
+      return;
+    }
   double s[2];
   const int ks[2] = { kTS, kTT };
   sum_parts<2> (a.part, a.grid, ks, s);
@@ -467,7 +583,7 @@ __global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
       sh_omega = isfinite (omega) ? omega : NAN;
       if (blockIdx.x == 0 && !isfinite (omega))
         {
-          // Leave x untouched so the caller keeps the last finite iterate.
+          // Leave x' untouched so the run keeps the last finite iterate.
           st->status = kStateBreakdown;
           *reinterpret_cast<volatile int *> (&st->done) = 1;
         }
@@ -477,7 +593,9 @@ __global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
   if (!isfinite (omega))
     return;
   const T ta = (T) sh_alpha, tw = (T) omega;
-  T rhr = 0, rr = 0;
+  // (x', x') feeds the replacement bound only: skipped (0) when it is off.
+  const bool track = st->eps > 0.0;
+  T rhr = 0, rr = 0, xx = 0;
   const T *qa = PRE ? a.q : a.p;
   const T *za = PRE ? a.z : a.s;
   const int64_t stride = (int64_t) gridDim.x * blockDim.x;
@@ -489,7 +607,7 @@ __global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
       for (int u = 0; u < 4; u++)
         {
           const int64_t k = i + u * stride;
-          xv[u] = a.x[k];
+          xv[u] = a.xp[k];
           qv[u] = qa[k];
           zv[u] = za[k];
           sv[u] = a.s[k];
@@ -501,30 +619,83 @@ __global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
       for (int u = 0; u < 4; u++)
         {
           const int64_t k = i + u * stride;
-          a.x[k] = xv[u] + ta * qv[u] + tw * zv[u]; // h = x + alpha q; x = h + omega z
-          const T ri = sv[u] - tw * tv[u];           // :340-357
+          const T xn = xv[u] + ta * qv[u] + tw * zv[u]; // h = x + alpha q; x = h + omega z
+          a.xp[k] = xn;
+          const T ri = sv[u] - tw * tv[u];              // :340-357
           a.r[k] = ri;
           rhr = fma (hv[u], ri, rhr);
           rr = fma (ri, ri, rr);
+          if (track)
+            xx = fma (xn, xn, xx);
         }
     }
   for (; i < a.n; i += stride)
     {
-      a.x[i] = a.x[i] + ta * qa[i] + tw * za[i];
+      const T xn = a.xp[i] + ta * qa[i] + tw * za[i];
+      a.xp[i] = xn;
       const T ri = a.s[i] - tw * a.t[i];
       a.r[i] = ri;
       rhr = fma (a.rh[i], ri, rhr);
       rr = fma (ri, ri, rr);
+      if (track)
+        xx = fma (xn, xn, xx);
     }
-  double vals[2] = { (double) rhr, (double) rr };
-  const int kk[2] = { kRhR, kRR };
-  store_parts<2> (vals, a.part, a.grid, kk);
+  double vals[3] = { (double) rhr, (double) rr, (double) xx };
+  const int kk[3] = { kRhR, kRR, kXX };
+  store_parts<3> (vals, a.part, a.grid, kk);
   if (blockIdx.x == 0 && threadIdx.x == 0)
     {
       st->omega = omega;
       st->rho_prev = st->rho;
       st->iter = st->iter + 1;
+      st->rep_done = 0;
+      st->dslot = st->dslot ^ 1;
     }
+}
+
+// End of a run: x = e (a fresh solve) or x += e (a restart), with e the run's
+// result g + x' or, when a snapshot is restored, the snapshot.
+template <typename T>
+__global__ void finish_kernel (int64_t n, T *x, const T *g, const T *xp, const T *snap, int add)
+{
+  GRID_STRIDE (i, n)
+  {
+    const T e = snap ? snap[i] : g[i] + xp[i];
+    x[i] = add ? x[i] + e : e;
+  }
+}
+
+// The run's current iterate g + x' into snap (the best-point copy).
+template <typename T> __global__ void snapshot_kernel (int64_t n, const T *g, const T *xp, T *snap)
+{
+  GRID_STRIDE (i, n)
+  snap[i] = g[i] + xp[i];
+}
+
+// cA = (entries per scalar row) * ||A||_inf, maxima over rows by atomics on
+// the bit patterns (non-negative doubles order like their bits).
+template <typename T>
+__global__ void row_norm_kernel (int nbr, int bs, const int *rp, const T *vals, unsigned long long *max_abs,
+                                 int *max_count)
+{
+  const int b = bs > 0 ? bs : 1;
+  GRID_STRIDE (i, (int64_t) nbr * b)
+  {
+    const int br = (int) (i / b), r = (int) (i % b);
+    double sum = 0.0;
+    int count = 0;
+    for (int k = rp[br]; k < rp[br + 1]; k++)
+      {
+        if (bs > 0)
+          for (int c = 0; c < bs; c++)
+            sum += fabs ((double) vals[(size_t) k * bs * bs + (size_t) r * bs + c]);
+        else
+          sum += fabs ((double) vals[k]);
+        count += b;
+      }
+    atomicMax (max_abs, (unsigned long long) __double_as_longlong (sum));
+    atomicMax (max_count, count);
+  }
 }
 
 // Point Jacobi from the diagonal blocks: P = 1/a_rr (1 when |a_rr| < 1e-20
@@ -632,7 +803,8 @@ void launch_residual (int kind, const Args<T> &a, const T *x, const T *b, T *r, 
 
 template <typename T>
 Args<T> make_args (const bmfp_matrix_s *A, int64_t n, void *x, void *r, void *rh, void *p, void *v,
-                   void *q, void *s, void *z, void *t, void *P, double *part, int grid, DevState *st)
+                   void *q, void *s, void *z, void *t, void *P, void *g, void *xp, double *part, int grid,
+                   DevState *st)
 {
   Args<T> a;
   a.nbr = A->n_rows;
@@ -651,6 +823,8 @@ Args<T> make_args (const bmfp_matrix_s *A, int64_t n, void *x, void *r, void *rh
   a.z = (T *) z;
   a.t = (T *) t;
   a.P = (const T *) P;
+  a.g = (T *) g;
+  a.xp = (T *) xp;
   a.part = part;
   a.grid = grid;
   a.st = st;
@@ -667,6 +841,42 @@ void launch_vector_phase (int phase, const Args<T> &a, cudaStream_t s)
   else
     phase_x<T, PRE><<<a.grid, kThreads, 0, s>>> (a);
 }
+
+// Unit roundoff of the engine's precision (replacement bound).
+double unit_roundoff (int dtype) { return dtype == BMFP_R64F ? 0x1p-53 : 0x1p-24; }
+
+// cA = max entries per scalar row * max absolute row sum of A (synchronises).
+int matrix_bound (const bmfp_matrix_s *A, int grid, double *cA, cudaStream_t s)
+{
+  struct Maxima
+  {
+    unsigned long long abs_bits;
+    int count;
+  };
+  Maxima *d = nullptr;
+  BMFP_CUDA (cudaMallocAsync (&d, sizeof (Maxima), s));
+  BMFP_CUDA (cudaMemsetAsync (d, 0, sizeof (Maxima), s));
+  if (A->dtype == BMFP_R64F)
+    row_norm_kernel<double><<<grid, kThreads, 0, s>>> (A->n_rows, A->bs, A->d_row_ptr, (const double *) A->d_vals,
+                                                        &d->abs_bits, &d->count);
+  else
+    row_norm_kernel<float><<<grid, kThreads, 0, s>>> (A->n_rows, A->bs, A->d_row_ptr, (const float *) A->d_vals,
+                                                       &d->abs_bits, &d->count);
+  cudaError_t e = cudaGetLastError ();
+  Maxima h{};
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync (&h, d, sizeof (Maxima), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync (d, s);
+  if (e == cudaSuccess)
+    e = cudaStreamSynchronize (s);
+  if (e != cudaSuccess)
+    return cuda_fail (e, "matrix_bound", __FILE__, __LINE__);
+  double amax;
+  const long long bits = (long long) h.abs_bits;
+  std::memcpy (&amax, &bits, sizeof amax);
+  *cA = (double) h.count * amax;
+  return BMFP_SUCCESS;
+}
 } // namespace
 
 // ------------------------------------------------------------ WideEngine
@@ -680,7 +890,7 @@ WideEngine::~WideEngine ()
   for (cudaEvent_t e : ev_)
     if (e)
       cudaEventDestroy (e);
-  for (void *ptr : { x_, r_, rh_, p_, v_, q_, s_, z_, t_, P_ })
+  for (void *ptr : { x_, r_, rh_, p_, v_, q_, s_, z_, t_, P_, g_, xp_ })
     cudaFree (ptr);
   cudaFree (part_);
   cudaFree (state_);
@@ -700,6 +910,7 @@ int WideEngine::init (const bmfp_matrix_s *A, bool jacobi, int chunk, cudaStream
   A_ = A;
   dtype_ = A->dtype;
   jacobi_ = jacobi;
+  replace_ = dtype_ == BMFP_R64F;
   chunk_ = std::max (1, std::min (chunk, 256));
   n_ = (int64_t) A->n_rows * bs;
   spmv_kind_ = spmv_kind_for (A);
@@ -712,8 +923,9 @@ int WideEngine::init (const bmfp_matrix_s *A, bool jacobi, int chunk, cudaStream
   grid_ = (int) std::min<int64_t> ((int64_t) sms * std::max (1, std::min (ctas_per_sm, 8)), want);
   const size_t S = dtype_size (dtype_);
   const size_t vb = S * (size_t) std::max<int64_t> (n_, 1);
-  for (void **ptr : { &x_, &r_, &rh_, &p_, &v_, &s_, &t_ })
+  for (void **ptr : { &x_, &r_, &rh_, &p_, &v_, &s_, &t_, &g_, &xp_ })
     BMFP_CUDA (cudaMalloc (ptr, vb));
+  BMFP_CUDA (cudaMemsetAsync (x_, 0, vb, stream));
   if (jacobi_)
     {
       BMFP_CUDA (cudaMalloc (&q_, vb));
@@ -740,7 +952,9 @@ int WideEngine::init (const bmfp_matrix_s *A, bool jacobi, int chunk, cudaStream
   BMFP_CUDA (cudaEventCreateWithFlags (&ev_[0], cudaEventDisableTiming));
   BMFP_CUDA (cudaEventCreateWithFlags (&ev_[1], cudaEventDisableTiming));
   BMFP_CUDA (cudaStreamCreateWithFlags (&capture_stream_, cudaStreamNonBlocking));
-  BMFP_CUDA (cudaStreamSynchronize (stream));
+  int rc = matrix_bound (A, grid_, &cA_, stream); // synchronises the stream
+  if (rc != BMFP_SUCCESS)
+    return rc;
   return capture (capture_stream_);
 }
 
@@ -750,7 +964,8 @@ int WideEngine::launch_phase (int phase, cudaStream_t s)
   void *z = jacobi_ ? z_ : s_;
   if (dtype_ == BMFP_R64F)
     {
-      Args<double> a = make_args<double> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, part_, grid_, state_);
+      Args<double> a
+        = make_args<double> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, g_, xp_, part_, grid_, state_);
       if (phase == 2 || phase == 4)
         launch_spmv_dispatch<double> (spmv_kind_, phase, a, s);
       else if (jacobi_)
@@ -760,7 +975,8 @@ int WideEngine::launch_phase (int phase, cudaStream_t s)
     }
   else
     {
-      Args<float> a = make_args<float> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, part_, grid_, state_);
+      Args<float> a
+        = make_args<float> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, g_, xp_, part_, grid_, state_);
       if (phase == 2 || phase == 4)
         launch_spmv_dispatch<float> (spmv_kind_, phase, a, s);
       else if (jacobi_)
@@ -796,37 +1012,48 @@ int WideEngine::capture (cudaStream_t s)
   return BMFP_SUCCESS;
 }
 
-int WideEngine::start_zero (const void *d_b, double tol, int max_iter, cudaStream_t s)
+int WideEngine::start (bool zero, const void *c, double tol, int max_iter, double norm_b, int iter0, cudaStream_t s)
 {
   void *q = jacobi_ ? q_ : p_;
   void *z = jacobi_ ? z_ : s_;
+  const double eps = replace_ ? unit_roundoff (dtype_) : 0.0;
+  c_ = c;
+  from_zero_ = zero;
   if (dtype_ == BMFP_R64F)
-    start_kernel<double, true><<<grid_, kThreads, 0, s>>> (
-      make_args<double> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, part_, grid_, state_),
-      (const double *) d_b, tol, max_iter, -1.0, 0);
+    {
+      const Args<double> a
+        = make_args<double> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, g_, xp_, part_, grid_, state_);
+      if (zero)
+        start_kernel<double, true><<<grid_, kThreads, 0, s>>> (a, (const double *) c, tol, max_iter, norm_b, iter0,
+                                                                eps, cA_);
+      else
+        start_kernel<double, false><<<grid_, kThreads, 0, s>>> (a, (const double *) c, tol, max_iter, norm_b,
+                                                                 iter0, eps, cA_);
+    }
   else
-    start_kernel<float, true><<<grid_, kThreads, 0, s>>> (
-      make_args<float> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, part_, grid_, state_),
-      (const float *) d_b, tol, max_iter, -1.0, 0);
+    {
+      const Args<float> a
+        = make_args<float> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, g_, xp_, part_, grid_, state_);
+      if (zero)
+        start_kernel<float, true><<<grid_, kThreads, 0, s>>> (a, (const float *) c, tol, max_iter, norm_b, iter0,
+                                                               eps, cA_);
+      else
+        start_kernel<float, false><<<grid_, kThreads, 0, s>>> (a, (const float *) c, tol, max_iter, norm_b, iter0,
+                                                                eps, cA_);
+    }
   BMFP_LAUNCH_CHECK ();
   return BMFP_SUCCESS;
+}
+
+int WideEngine::start_zero (const void *d_b, double tol, int max_iter, cudaStream_t s)
+{
+  return start (true, d_b, tol, max_iter, -1.0, 0, s);
 }
 
 int WideEngine::start_residual (const void *d_r, double tol, int max_iter_total, double norm_b,
                                 cudaStream_t s, int iter0)
 {
-  void *q = jacobi_ ? q_ : p_;
-  void *z = jacobi_ ? z_ : s_;
-  if (dtype_ == BMFP_R64F)
-    start_kernel<double, false><<<grid_, kThreads, 0, s>>> (
-      make_args<double> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, part_, grid_, state_),
-      (const double *) d_r, tol, max_iter_total, norm_b, iter0);
-  else
-    start_kernel<float, false><<<grid_, kThreads, 0, s>>> (
-      make_args<float> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, part_, grid_, state_),
-      (const float *) d_r, tol, max_iter_total, norm_b, iter0);
-  BMFP_LAUNCH_CHECK ();
-  return BMFP_SUCCESS;
+  return start (false, d_r, tol, max_iter_total, norm_b, iter0, s);
 }
 
 namespace
@@ -845,9 +1072,9 @@ int WideEngine::run (cudaStream_t s, DevState *out, void *d_snap, double *snap_r
   // Keep one graph in flight while the host inspects the previous one.
   long k = 0;
   const long limit = 1 + (long) 1e9 / chunk_;
-  const size_t xbytes = dtype_size (dtype_) * (size_t) n_;
   double best = INFINITY;                              // smallest (r, r) polled
-  double snap_at = snap_rr ? *snap_rr : INFINITY;      // (r, r) of the last copy
+  const double snap_in = snap_rr ? *snap_rr : INFINITY;
+  double snap_at = snap_in;                            // (r, r) of the last copy
   long snap_k = -1;                                    // graph whose end the copy holds
   double mark = INFINITY;                              // best (r, r) at the last halving
   int mark_it = 0;                                     // iteration of that halving
@@ -867,10 +1094,17 @@ int WideEngine::run (cudaStream_t s, DevState *out, void *d_snap, double *snap_r
             break;
           if (h.rr < best)
             best = h.rr;
-          // x after graph k (queued behind it); its (r, r) is read next poll.
+          // The iterate after graph k (queued behind it); its (r, r) is read
+          // at the next poll.
           if (d_snap && snap_rr && h.rr < 0.25 * snap_at && snap_k != k - 1)
             {
-              BMFP_CUDA (cudaMemcpyAsync (d_snap, x_, xbytes, cudaMemcpyDeviceToDevice, s));
+              if (dtype_ == BMFP_R64F)
+                snapshot_kernel<double><<<grid_, kThreads, 0, s>>> (n_, (const double *) g_, (const double *) xp_,
+                                                                     (double *) d_snap);
+              else
+                snapshot_kernel<float><<<grid_, kThreads, 0, s>>> (n_, (const float *) g_, (const float *) xp_,
+                                                                    (float *) d_snap);
+              BMFP_LAUNCH_CHECK ();
               snap_k = k;
               snap_at = h.rr;
             }
@@ -896,6 +1130,20 @@ int WideEngine::run (cudaStream_t s, DevState *out, void *d_snap, double *snap_r
   *out = h_state_[k & 1];
   if (snap_k == k && snap_rr)
     *snap_rr = out->rr;
+  // The run's result into x: the snapshot when the run ended above the best
+  // point it passed (and that point is a copy of this run), else g + x'.
+  const bool restore = d_snap && snap_rr && snap_k >= 0 && out->status != kStateConverged && *snap_rr < snap_in
+                       && !(out->rr <= *snap_rr);
+  if (restore)
+    out->rr = *snap_rr;
+  const int add = from_zero_ ? 0 : 1;
+  if (dtype_ == BMFP_R64F)
+    finish_kernel<double><<<grid_, kThreads, 0, s>>> (n_, (double *) x_, (const double *) g_, (const double *) xp_,
+                                                       restore ? (const double *) d_snap : nullptr, add);
+  else
+    finish_kernel<float><<<grid_, kThreads, 0, s>>> (n_, (float *) x_, (const float *) g_, (const float *) xp_,
+                                                      restore ? (const float *) d_snap : nullptr, add);
+  BMFP_LAUNCH_CHECK ();
   return BMFP_SUCCESS;
 }
 
@@ -903,13 +1151,15 @@ int WideEngine::true_residual (const void *d_b, void *d_r, double *rr, double *b
 {
   if (dtype_ == BMFP_R64F)
     {
-      Args<double> a = make_args<double> (A_, n_, x_, r_, rh_, p_, v_, p_, s_, s_, t_, P_, part_, grid_, state_);
+      Args<double> a
+        = make_args<double> (A_, n_, x_, r_, rh_, p_, v_, p_, s_, s_, t_, P_, g_, xp_, part_, grid_, state_);
       launch_residual<double> (spmv_kind_, a, (const double *) x_, (const double *) d_b, (double *) d_r,
                                (double *) t_, s);
     }
   else
     {
-      Args<float> a = make_args<float> (A_, n_, x_, r_, rh_, p_, v_, p_, s_, s_, t_, P_, part_, grid_, state_);
+      Args<float> a
+        = make_args<float> (A_, n_, x_, r_, rh_, p_, v_, p_, s_, s_, t_, P_, g_, xp_, part_, grid_, state_);
       launch_residual<float> (spmv_kind_, a, (const float *) x_, (const float *) d_b, (float *) d_r,
                               (float *) t_, s);
     }
@@ -931,7 +1181,8 @@ int WideEngine::true_residual (const void *d_b, void *d_r, double *rr, double *b
 // ------------------------------------------------------------ raw buffers
 // Launchers over caller-provided buffers, for the entry point that
 // allocates nothing (noalloc.cu). They run the same phase kernels as
-// WideEngine, without graphs.
+// WideEngine, without graphs, and without residual replacement (the
+// reference's plain recurrences).
 
 int raw_solve_grid (int64_t n, int *grid)
 {
@@ -959,7 +1210,7 @@ template <typename T> Args<T> raw_args (const RawSolve &b)
 {
   void *q = b.jacobi ? b.q : b.p;
   void *z = b.jacobi ? b.z : b.s;
-  return make_args<T> (&b.A, b.n, b.x, b.r, b.rh, b.p, b.v, q, b.s, z, b.t, b.P, b.part, b.grid, b.st);
+  return make_args<T> (&b.A, b.n, b.x, b.r, b.rh, b.p, b.v, q, b.s, z, b.t, b.P, b.g, b.xp, b.part, b.grid, b.st);
 }
 } // namespace
 
@@ -980,10 +1231,10 @@ int raw_start (const RawSolve &b, const void *d_rhs, double tol, int max_iter, c
 {
   if (b.A.dtype == BMFP_R64F)
     start_kernel<double, true><<<b.grid, kThreads, 0, s>>> (raw_args<double> (b), (const double *) d_rhs,
-                                                            tol, max_iter, -1.0, 0);
+                                                            tol, max_iter, -1.0, 0, 0.0, 0.0);
   else
     start_kernel<float, true><<<b.grid, kThreads, 0, s>>> (raw_args<float> (b), (const float *) d_rhs,
-                                                           tol, max_iter, -1.0, 0);
+                                                           tol, max_iter, -1.0, 0, 0.0, 0.0);
   BMFP_LAUNCH_CHECK ();
   return BMFP_SUCCESS;
 }
@@ -1011,6 +1262,18 @@ int raw_phase (const RawSolve &b, int phase, cudaStream_t s)
       else
         launch_vector_phase<float, false> (phase, a, s);
     }
+  BMFP_LAUNCH_CHECK ();
+  return BMFP_SUCCESS;
+}
+
+int raw_finish (const RawSolve &b, cudaStream_t s)
+{
+  if (b.A.dtype == BMFP_R64F)
+    finish_kernel<double><<<b.grid, kThreads, 0, s>>> (b.n, (double *) b.x, (const double *) b.g,
+                                                       (const double *) b.xp, nullptr, 0);
+  else
+    finish_kernel<float><<<b.grid, kThreads, 0, s>>> (b.n, (float *) b.x, (const float *) b.g, (const float *) b.xp,
+                                                      nullptr, 0);
   BMFP_LAUNCH_CHECK ();
   return BMFP_SUCCESS;
 }

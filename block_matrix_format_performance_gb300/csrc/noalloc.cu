@@ -6,13 +6,16 @@
 // host application owns every allocation. bmfp_bicgstab_solve_noalloc takes
 // the matrix, the right-hand side and the solution buffer from the caller and
 // keeps every other vector of the solve in one file-scope device array,
-// g_noalloc_scratch, of fixed size (kNoAllocScratchBytes, about 9.5 MB). Every
+// g_noalloc_scratch, of fixed size (kNoAllocScratchBytes, about 11.6 MB). Every
 // GPU that loads the library holds that array until the process exits.
 //
 // Host code cannot use the array's name as a device address (in host code it
 // names a host-side stand-in), so the first call on each device, with that
 // device current, looks the address up with cudaGetSymbolAddress and caches
-// it. That first call should come before any stream capture.
+// it. That first call should come before any stream capture. The cached
+// address belongs to the device's context: a caller that resets the device
+// (cudaDeviceReset) after a call must not call this entry point again in the
+// same process.
 //
 // All calls share the one array and it keeps the previous call's contents:
 // every solve re-initialises what it reads (the start kernel writes every
@@ -32,7 +35,7 @@ namespace
 {
 constexpr int64_t kNoAllocMaxRows = 131072; // scalar rows (DOFs) per solve
 constexpr int kNoAllocMaxGrid = 1024;       // CTAs of the phase kernels
-constexpr int kNoAllocVectors = 9;          // r, rh, p, v, s, t, q, z, P
+constexpr int kNoAllocVectors = 11;         // r, rh, p, v, s, t, q, z, P, g, x'
 constexpr size_t kVectorSlot = (size_t) kNoAllocMaxRows * sizeof (double); // 256-byte multiple
 constexpr size_t kPartsBytes = (size_t) kRawParts * kNoAllocMaxGrid * sizeof (double);
 constexpr size_t kStateSlot = 256;
@@ -88,6 +91,11 @@ extern "C" int bmfp_bicgstab_solve_noalloc (int dtype, int n_block_rows, int bs,
     return fail (BMFP_ERROR_NOT_SUPPORTED,
                  "%lld rows exceed the no-allocation scratch limit of %lld rows; use bmfp_solver_create",
                  (long long) n, (long long) kNoAllocMaxRows);
+  // The phase kernels index values with 32-bit block offsets times bs^2, as
+  // the matrix handles do (bmfp_matrix_create_bcsr refuses the same).
+  const int64_t bsq = (int64_t) (bs ? bs : 1) * (bs ? bs : 1);
+  if (nnzb > INT32_MAX || nnzb * bsq > INT32_MAX)
+    return fail (BMFP_ERROR_NOT_SUPPORTED, "%lld stored values exceed 2^31 - 1", (long long) (nnzb * bsq));
   if (n == 0)
     return BMFP_SUCCESS;
   if (!d_row_ptr || !d_b || !d_x || (nnzb > 0 && (!d_cols || !d_values)))
@@ -116,7 +124,7 @@ extern "C" int bmfp_bicgstab_solve_noalloc (int dtype, int n_block_rows, int bs,
     return rc;
   if (b.grid > kNoAllocMaxGrid)
     b.grid = kNoAllocMaxGrid;
-  void **vecs[kNoAllocVectors] = { &b.r, &b.rh, &b.p, &b.v, &b.s, &b.t, &b.q, &b.z, &b.P };
+  void **vecs[kNoAllocVectors] = { &b.r, &b.rh, &b.p, &b.v, &b.s, &b.t, &b.q, &b.z, &b.P, &b.g, &b.xp };
   for (int i = 0; i < kNoAllocVectors; i++)
     *vecs[i] = base + (size_t) i * kVectorSlot;
   b.part = reinterpret_cast<double *> (base + kNoAllocVectors * kVectorSlot);
@@ -143,6 +151,10 @@ extern "C" int bmfp_bicgstab_solve_noalloc (int dtype, int n_block_rows, int bs,
       if (h.done)
         break;
     }
+  // The iterate accumulated in the array (x' of the run) into the caller's x.
+  if ((rc = raw_finish (b, s)) != BMFP_SUCCESS)
+    return rc;
+  BMFP_CUDA (cudaStreamSynchronize (s));
   if (iterations)
     *iterations = h.iter;
   if (rel_residual)

@@ -159,7 +159,7 @@ size_t request_bytes (const bmfp_server_s *sv, int64_t n, bool wide)
 {
   if (wide)
     return (size_t) n * 8 * 15; // solver vectors (work and Krylov) + b, x
-  size_t b = align256 (n * 8) * 2 + align256 (n * 8 * 9); // b, x, 9 FP64 work vectors
+  size_t b = align256 (n * 8) * 2 + align256 (n * 8 * kBatchW64); // b, x, FP64 work vectors
   if (sv->opts.solver.precision != BMFP_SOLVE_FP64)
     b += align256 (n * 4 * 8); // 8 FP32 work vectors
   return b;
@@ -262,7 +262,7 @@ int launch_micro_batch (bmfp_server_s *sv, std::vector<Request *> &reqs, int str
       r->d_x = (double *) p;
       p += align256 (r->n * 8);
       r->w64 = (double *) p;
-      p += align256 (r->n * 8 * 9);
+      p += align256 (r->n * 8 * kBatchW64);
       if (sv->opts.solver.precision != BMFP_SOLVE_FP64)
         {
           r->w32 = (float *) p;
@@ -337,6 +337,7 @@ void take_request (bmfp_server_s *sv, MicroBatch *mb, size_t i, bool ok)
   f.iterations_fp32 = o.iterations_fp32;
   f.refinements = o.refinements;
   f.restarts = o.restarts;
+  f.replacements = o.replacements;
   f.used_fp64_fallback = o.fallback;
   f.true_rel_residual = o.true_rel;
   f.recursive_rel_residual = o.rec_rel;

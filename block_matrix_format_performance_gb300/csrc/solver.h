@@ -11,6 +11,19 @@ namespace bmfp
 {
 // Device-resident scalars of one BiCGStab solve. Every phase kernel reads
 // only fields written by earlier kernels, so no kernel races with itself.
+//
+// Residual replacement (H. A. van der Vorst and Q. Ye, "Residual replacement
+// strategies for Krylov subspace iterative methods for the convergence of
+// true residuals", SIAM J. Sci. Comput. 22, 2000; the variant with group
+// update): dev bounds the deviation between the recursive residual r and the
+// true b - A x that rounding has accumulated since the last replacement,
+//   dev_i = dev_{i-1} + eps (cA ||x'_i|| + ||r_i||),
+// with x' the updates accumulated since then and cA = (entries per row) *
+// ||A||_inf. When dev crosses kReplaceThreshold * ||r|| (from below, and
+// dev > 1.1 dev0), the accumulated updates are folded into the group base g
+// and r is replaced by the true residual c - A g. This keeps the recursive
+// residual honest near convergence, so a solve stopped on it meets the
+// tolerance in b - A x as well.
 struct DevState
 {
   double rho;      // (rh, r) of the current iteration (phase 1)
@@ -20,11 +33,28 @@ struct DevState
   double norm_b;   // ||r0|| (phase 1, first iteration)
   double rr;       // last (r, r) seen by phase 1
   double tol;      // stop when sqrt(rr) / norm_b < tol
+  double eps;      // unit roundoff of the working precision; 0 = no replacement
+  double cA;       // max entries per scalar row * max absolute row sum
+  // Deviation bound since the last replacement, its value at that
+  // replacement, and ||r|| of the previous iteration: phase 1 reads slot
+  // dslot and writes slot dslot ^ 1 (other CTAs of phase 1 still read the
+  // old values), phase 5 flips dslot.
+  double dev[2], dev0[2], nr_prev[2];
+  const void *c;   // right-hand side of the run (b, or a restart's residual)
   int iter;        // iterations completed (phase 5)
   int max_iter;
   int done;        // set by phase 1; every kernel returns early once set
   int status;      // 0 running, 1 converged, 2 iteration limit, 3 breakdown
+  int rep_now;     // phase 1 chose to replace r this iteration (read by phases 2-5)
+  int rep_done;    // the iteration phase 5 just closed was a replacement (read by phase 1)
+  int replacements;
+  int dslot;
 };
+
+// Replacement threshold on dev / ||r|| (van der Vorst and Ye use sqrt(eps);
+// 1e-3 measured best on the Q4 elasticity family: every grid up to 400x100
+// ends below 1e-10 in b - A x with one to three replacements).
+constexpr double kReplaceThreshold = 1e-3;
 
 enum
 {
@@ -38,6 +68,12 @@ enum
 // each over all rows with a fixed persistent grid, captured in a CUDA graph
 // of `chunk` iterations. Dot products are per-CTA partials summed in a fixed
 // order by the next phase, so a solve is deterministic for a given grid.
+//
+// Every run solves A e = c from e = 0 (c = b for a fresh solve, c = the true
+// residual for a restart): the updates accumulate in xp, are folded into the
+// group base g at each residual replacement, and the run's result g + xp
+// goes into x when the run ends (x = e for a fresh solve, x += e for a
+// restart). Between runs x holds the solution.
 class WideEngine
 {
 public:
@@ -47,22 +83,30 @@ public:
   WideEngine &operator= (const WideEngine &) = delete;
 
   int init (const bmfp_matrix_s *A, bool jacobi, int chunk, cudaStream_t stream, int ctas_per_sm = 4);
-  // Start a solve of A x = b from x0 = 0 (b on the device, engine dtype).
+  // Residual replacement on (default for FP64 engines) or off (the
+  // reference's plain recurrences; FP32 engines always run without it).
+  void set_replacement (bool on) { replace_ = on && dtype_ == BMFP_R64F; }
+  // Start a solve of A x = b from x0 = 0 (b on the device, engine dtype; it
+  // must stay valid until the run ends: replacements read it).
   int start_zero (const void *d_b, double tol, int max_iter, cudaStream_t stream);
-  // Restart from the current x with the residual given in d_r (true residual).
+  // Restart from the current x with the residual given in d_r (true residual;
+  // kept until the run ends, as d_b above).
   // norm_b > 0 sets the reference norm of the convergence test (an engine that
   // never ran start_zero has none); norm_b <= 0 keeps the previous one.
   // iter0 >= 0 restarts the iteration count there (a new solve on an engine
   // whose last run belonged to an earlier one); -1 keeps counting.
   int start_residual (const void *d_r, double tol, int max_iter_total, double norm_b,
                       cudaStream_t stream, int iter0 = -1);
-  // Runs graphs until the device sets done; returns the final state. With
-  // d_snapshot, x is copied there each time the recursive residual has
-  // fallen 4x below the last copy (and below snapshot_rr on entry), and
-  // *snapshot_rr receives the (r, r) of the copy; a residual that grows
-  // 1e8-fold over the best seen, or turns non-finite, stops the run as a
-  // breakdown, and so does (stall > 0) a best residual that has not halved
-  // within `stall` iterations of the start or of its last halving.
+  // Runs graphs until the device sets done, then writes the run's result
+  // into x; returns the final state. With d_snapshot, the run's iterate is
+  // copied there each time the recursive residual has fallen 4x below the
+  // last copy (and below snapshot_rr on entry), and *snapshot_rr receives
+  // the (r, r) of the copy; a run that ends above that point (breakdown,
+  // iteration limit on an erratic stretch) returns the copy instead, with
+  // out->rr set to its (r, r). A residual that grows 1e16-fold over the best
+  // seen, or turns non-finite, stops the run as a breakdown, and so does
+  // (stall > 0) a best residual that has not halved within `stall`
+  // iterations of the start or of its last halving.
   int run (cudaStream_t stream, DevState *out, void *d_snapshot = nullptr, double *snapshot_rr = nullptr,
            int stall = 0);
   // r = b - A x, returns ||r||^2 and ||b||^2 (synchronises the stream).
@@ -77,16 +121,22 @@ public:
 private:
   int capture (cudaStream_t stream);
   int launch_phase (int phase, cudaStream_t stream);
+  int start (bool zero, const void *c, double tol, int max_iter, double norm_b, int iter0, cudaStream_t s);
 
   const bmfp_matrix_s *A_ = nullptr;
   int dtype_ = BMFP_R64F;
   bool jacobi_ = false;
+  bool replace_ = true;
+  bool from_zero_ = true; // the current run started from x = 0
   int64_t n_ = 0;
   int grid_ = 0;
   int chunk_ = 16;
   int spmv_kind_ = 0;
+  double cA_ = 0.0; // entries per row * ||A||_inf (replacement bound)
+  const void *c_ = nullptr; // right-hand side of the current run
   void *x_ = nullptr, *r_ = nullptr, *rh_ = nullptr, *p_ = nullptr, *v_ = nullptr;
   void *q_ = nullptr, *s_ = nullptr, *z_ = nullptr, *t_ = nullptr, *P_ = nullptr;
+  void *g_ = nullptr, *xp_ = nullptr;
   double *part_ = nullptr;
   DevState *state_ = nullptr;
   DevState *h_state_ = nullptr; // pinned, two slots
@@ -107,16 +157,19 @@ struct RawSolve
   bool aligned = true; // values 16-byte aligned: the vectorised SpMV may run
   void *x = nullptr, *r = nullptr, *rh = nullptr, *p = nullptr, *v = nullptr;
   void *q = nullptr, *s = nullptr, *z = nullptr, *t = nullptr, *P = nullptr;
+  void *g = nullptr, *xp = nullptr; // group base and accumulated updates of the run
   double *part = nullptr; // kRawParts * grid doubles
   DevState *st = nullptr;
 };
-constexpr int kRawParts = 7;
+constexpr int kRawParts = 9;
 
 // Grid of the phase kernels for n rows (the same rule as WideEngine).
 int raw_solve_grid (int64_t n, int *grid);
 int raw_jacobi (const RawSolve &b, cudaStream_t stream);
 int raw_start (const RawSolve &b, const void *d_rhs, double tol, int max_iter, cudaStream_t stream);
 int raw_phase (const RawSolve &b, int phase, cudaStream_t stream);
+// x = g + xp: the run's result into the caller's x (after the last phase).
+int raw_finish (const RawSolve &b, cudaStream_t stream);
 
 // Elementwise helpers used by the refinement loop (vector_ops.cu).
 int axpy_scaled_convert (int dst_dtype, int src_dtype, int64_t n, double a, const void *src,

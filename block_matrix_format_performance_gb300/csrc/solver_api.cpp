@@ -3,10 +3,12 @@
 #include "batch.h"
 #include "solver.h"
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <memory>
 #include <new>
+#include <vector>
 
 using namespace bmfp;
 
@@ -21,7 +23,7 @@ struct bmfp_solver_s
   void *work_b = nullptr;
   void *work_c = nullptr;               // best iterate kept across restarts
   void *work_d = nullptr;               // best iterate within one run (WideEngine::run snapshot)
-  bool fp32_stalls = false;             // MIXED: an earlier solve had to finish in FP64
+  bool fp64_only = false;               // MIXED: the creation probe found FP32 steps unable to progress
 
   ~bmfp_solver_s ()
   {
@@ -47,34 +49,28 @@ int status_of (const DevState &st)
   return BMFP_ERROR_NOT_CONVERGED;
 }
 
-// Runs the engine and, when the run ends above the best point it passed (a
-// breakdown, a blow-up stopped by the engine, or the iteration limit reached
-// on an erratic stretch of the residual history), puts x back at that point.
-int run_keep_best (WideEngine &e, void *d_snap, DevState *st, cudaStream_t s)
+// Runs the engine with its best-point snapshot: a run that ends above the
+// best point it passed (a breakdown, a blow-up stopped by the engine, or the
+// iteration limit reached on an erratic stretch of the residual history)
+// returns that point. Counts the run's residual replacements into *reps.
+int run_keep_best (WideEngine &e, void *d_snap, DevState *st, cudaStream_t s, int *reps)
 {
   double snap_rr = INFINITY;
-  int rc = e.run (s, st, d_snap, &snap_rr);
-  if (rc != BMFP_SUCCESS)
-    return rc;
-  if (st->status != kStateConverged && snap_rr < INFINITY && !(st->rr <= snap_rr))
-    {
-      BMFP_CUDA (cudaMemcpyAsync (e.x (), d_snap, dtype_size (e.dtype ()) * (size_t) e.n (),
-                                  cudaMemcpyDeviceToDevice, s));
-      BMFP_CUDA (cudaStreamSynchronize (s));
-      st->rr = snap_rr;
-    }
-  return BMFP_SUCCESS;
+  const int rc = e.run (s, st, d_snap, &snap_rr);
+  if (rc == BMFP_SUCCESS && reps)
+    *reps += st->replacements;
+  return rc;
 }
 
 // Restart loop shared by the plain and the mixed solves: verify b - A x,
 // restart from the true residual while each restart still lowers it (at most
-// 8 times), and keep the best iterate: near the attainable accuracy of the working
-// precision a restart can leave x worse (asking the recursive residual for
-// less than the tolerance only makes that more likely, measured), and then x
-// is restored.
+// 8 times), and keep the best iterate: near the attainable accuracy of the
+// working precision a restart can leave x worse (the more so the lower it
+// aims: a tenth of its starting residual measured worse than half), and then
+// x is restored.
 int finish_with_restarts (WideEngine &e, const void *d_b, void *d_r, void *d_xbest, void *d_snap,
                           const bmfp_solver_options &o, DevState &st, int iter_budget, double norm_b,
-                          int *restarts_out, double *rel_out, cudaStream_t s)
+                          int *restarts_out, double *rel_out, int *reps, cudaStream_t s)
 {
   const size_t xbytes = dtype_size (e.dtype ()) * (size_t) e.n ();
   double best = INFINITY;
@@ -107,9 +103,13 @@ int finish_with_restarts (WideEngine &e, const void *d_b, void *d_r, void *d_xbe
         break;
       BMFP_CUDA (cudaMemcpyAsync (d_xbest, e.x (), xbytes, cudaMemcpyDeviceToDevice, s));
       restarts++;
-      rc = e.start_residual (d_r, o.tolerance, iter_budget, norm_b > 0 ? norm_b : std::sqrt (bb), s);
+      // Aim at half the true residual the restart starts from: asked only
+      // for the tolerance again, from just above it, a restart moves x by a
+      // hair and the true residual with it.
+      rc = e.start_residual (d_r, std::min (o.tolerance, 0.5 * rel), iter_budget,
+                             norm_b > 0 ? norm_b : std::sqrt (bb), s);
       if (rc == BMFP_SUCCESS)
-        rc = run_keep_best (e, d_snap, &st, s);
+        rc = run_keep_best (e, d_snap, &st, s, reps);
       if (rc != BMFP_SUCCESS)
         return rc;
     }
@@ -124,9 +124,10 @@ int solve_plain (WideEngine &e, const void *d_b, void *d_r, void *d_xbest, void 
                  const bmfp_solver_options &o, bmfp_solve_info *info, cudaStream_t s)
 {
   DevState st{};
+  int reps = 0;
   int rc = e.start_zero (d_b, o.tolerance, o.max_iterations, s);
   if (rc == BMFP_SUCCESS)
-    rc = run_keep_best (e, d_snap, &st, s);
+    rc = run_keep_best (e, d_snap, &st, s, &reps);
   if (rc != BMFP_SUCCESS)
     return rc;
   int status = status_of (st);
@@ -135,7 +136,7 @@ int solve_plain (WideEngine &e, const void *d_b, void *d_r, void *d_xbest, void 
   if (o.check_true_residual)
     {
       rc = finish_with_restarts (e, d_b, d_r, d_xbest, d_snap, o, st, o.max_iterations, -1.0, &restarts, &rel_true,
-                                 s);
+                                 &reps, s);
       if (rc != BMFP_SUCCESS)
         return rc;
       status = rel_true < o.tolerance ? BMFP_SUCCESS
@@ -144,6 +145,7 @@ int solve_plain (WideEngine &e, const void *d_b, void *d_r, void *d_xbest, void 
   info->status = status;
   info->iterations += st.iter;
   info->restarts += restarts;
+  info->replacements += reps;
   info->true_rel_residual = rel_true;
   info->recursive_rel_residual = st.norm_b > 0 ? std::sqrt (st.rr) / st.norm_b : 0.0;
   return BMFP_SUCCESS;
@@ -153,7 +155,9 @@ int solve_plain (WideEngine &e, const void *d_b, void *d_r, void *d_xbest, void 
 // to ||b||) when they fall back finish in FP64 from x = 0.
 constexpr double kFreshFp64Above = 1e-2;
 
-int solve_mixed (bmfp_solver_s *sv, const void *d_b, bmfp_solve_info *info, cudaStream_t s)
+// probe: the creation probe's run (probe_fp32): the FP32 refinement phase
+// only, returning with used_fp64_fallback = 1 where a solve would fall back.
+int solve_mixed (bmfp_solver_s *sv, const void *d_b, bmfp_solve_info *info, cudaStream_t s, bool probe = false)
 {
   const bmfp_solver_options &o = sv->opts;
   WideEngine &e64 = *sv->main;
@@ -162,11 +166,11 @@ int solve_mixed (bmfp_solver_s *sv, const void *d_b, bmfp_solve_info *info, cuda
   void *r64 = sv->work_a; // FP64 residual
   void *r32 = sv->work_b; // scaled FP32 right-hand side of the inner solve
   BMFP_CUDA (cudaMemsetAsync (e64.x (), 0, sizeof (double) * (size_t) n, s));
-  if (sv->fp32_stalls && o.fallback_fp64)
+  if (sv->fp64_only && o.fallback_fp64)
     {
-      // An earlier solve on this matrix found the FP32 inner solves unable to
-      // make progress (its conditioning is beyond FP32's reach, and it does
-      // not change between right-hand sides): go straight to FP64.
+      // The creation probe found FP32 steps unable to make progress on this
+      // matrix (its conditioning is beyond FP32's reach, and it does not
+      // change between right-hand sides): go straight to FP64.
       int rc = solve_plain (e64, d_b, r64, sv->work_c, sv->work_d, o, info, s);
       info->used_fp64_fallback = 1;
       info->iterations_fp32 = 0;
@@ -190,6 +194,12 @@ int solve_mixed (bmfp_solver_s *sv, const void *d_b, bmfp_solve_info *info, cuda
         }
       const bool budget_left = iters64 + iters32 < o.max_iterations && k < o.max_refinements;
       const bool stalled = k > 0 && rel > prev_rel / 4;
+      if (probe && (!budget_left || stalled))
+        {
+          info->used_fp64_fallback = 1;
+          info->status = BMFP_ERROR_NOT_CONVERGED;
+          break;
+        }
       if (!budget_left || (stalled && o.fallback_fp64))
         {
           if (!o.fallback_fp64 || iters64 + iters32 >= o.max_iterations)
@@ -198,7 +208,6 @@ int solve_mixed (bmfp_solver_s *sv, const void *d_b, bmfp_solve_info *info, cuda
               break;
             }
           info->used_fp64_fallback = 1;
-          sv->fp32_stalls = true;
           if (rel > kFreshFp64Above)
             {
               // The FP32 steps gained less than 100x: finish with FP64 from
@@ -212,6 +221,7 @@ int solve_mixed (bmfp_solver_s *sv, const void *d_b, bmfp_solve_info *info, cuda
                 return rc;
               iters64 = i2.iterations;
               info->restarts += i2.restarts;
+              info->replacements += i2.replacements;
               info->true_rel_residual = i2.true_rel_residual;
               info->recursive_rel_residual = i2.recursive_rel_residual;
               info->status = i2.status;
@@ -221,15 +231,16 @@ int solve_mixed (bmfp_solver_s *sv, const void *d_b, bmfp_solve_info *info, cuda
           DevState st{};
           // A fresh count: this engine's device counter still holds the
           // last run of an earlier solve on the same solver.
+          int reps = 0;
           rc = e64.start_residual (r64, o.tolerance, o.max_iterations - iters32, std::sqrt (bb), s, 0);
           if (rc == BMFP_SUCCESS)
-            rc = run_keep_best (e64, sv->work_d, &st, s);
+            rc = run_keep_best (e64, sv->work_d, &st, s, &reps);
           if (rc != BMFP_SUCCESS)
             return rc;
           int restarts = 0;
           double rel_fin = NAN;
           rc = finish_with_restarts (e64, d_b, r64, sv->work_c, sv->work_d, o, st, o.max_iterations - iters32,
-                                     std::sqrt (bb), &restarts, &rel_fin, s);
+                                     std::sqrt (bb), &restarts, &rel_fin, &reps, s);
           if (rc != BMFP_SUCCESS)
             return rc;
           iters64 = st.iter;
@@ -239,6 +250,7 @@ int solve_mixed (bmfp_solver_s *sv, const void *d_b, bmfp_solve_info *info, cuda
                                                : (st.status == kStateBreakdown ? BMFP_ERROR_BREAKDOWN
                                                                                : BMFP_ERROR_NOT_CONVERGED);
           info->restarts += restarts;
+          info->replacements += reps;
           if (info->status == BMFP_ERROR_BREAKDOWN && iters32 + iters64 < o.max_iterations)
             {
               // BiCGStab from the refined iterate can break down again and
@@ -255,6 +267,7 @@ int solve_mixed (bmfp_solver_s *sv, const void *d_b, bmfp_solve_info *info, cuda
                 return rc;
               iters64 += i2.iterations;
               info->restarts += i2.restarts;
+              info->replacements += i2.replacements;
               if (i2.true_rel_residual < rel_fin)
                 {
                   info->true_rel_residual = i2.true_rel_residual;
@@ -296,6 +309,30 @@ int solve_mixed (bmfp_solver_s *sv, const void *d_b, bmfp_solve_info *info, cuda
   info->iterations_fp32 = iters32;
   return BMFP_SUCCESS;
 }
+// MIXED creation probe: solve_mixed's FP32 refinement phase on a seeded
+// right-hand side uniform in [-1, 1). FP32 steps are judged unable to finish
+// this matrix when that phase stops where a solve would fall back to FP64
+// (an inner solve that does not halve its residual, an outer step that cuts
+// the FP64 residual by less than 4x, or the budget spent).
+int probe_fp32 (bmfp_solver_s *sv, cudaStream_t s, bool *fp64_only)
+{
+  const int64_t n = sv->main->n ();
+  *fp64_only = false;
+  if (n == 0)
+    return BMFP_SUCCESS;
+  std::vector<double> h ((size_t) n);
+  int rc = bmfp_gen_uniform_vector (BMFP_R64F, n, 0x70726f6265ull, 0, h.data ());
+  if (rc != BMFP_SUCCESS)
+    return rc;
+  void *b = sv->work_c; // solve_mixed's refinement phase leaves work_c alone
+  BMFP_CUDA (cudaMemcpyAsync (b, h.data (), sizeof (double) * (size_t) n, cudaMemcpyHostToDevice, s));
+  bmfp_solve_info pi{};
+  rc = solve_mixed (sv, b, &pi, s, true);
+  if (rc != BMFP_SUCCESS)
+    return rc;
+  *fp64_only = pi.used_fp64_fallback != 0 || pi.status != BMFP_SUCCESS;
+  return BMFP_SUCCESS;
+}
 } // namespace
 
 extern "C" {
@@ -316,6 +353,7 @@ void bmfp_solver_options_init (bmfp_solver_options *o)
   o->iterations_per_graph = 16;
   o->ctas_per_sm = 4;
   o->inner_stall_iterations = 64;
+  o->residual_replacement = 1;
 }
 
 int bmfp_solver_create (bmfp_solver_t *out, bmfp_matrix_t A, const bmfp_solver_options *opts,
@@ -376,11 +414,20 @@ int bmfp_solver_create (bmfp_solver_t *out, bmfp_matrix_t A, const bmfp_solver_o
     }
   if (rc != BMFP_SUCCESS)
     return rc;
+  sv->main->set_replacement (o.residual_replacement != 0 && o.check_true_residual != 0);
   const size_t nb = (size_t) std::max (n_rows, 1);
   BMFP_CUDA (cudaMalloc (&sv->work_a, nb * 8));
   BMFP_CUDA (cudaMalloc (&sv->work_b, nb * 8));
   BMFP_CUDA (cudaMalloc (&sv->work_c, nb * 8));
   BMFP_CUDA (cudaMalloc (&sv->work_d, nb * 8));
+  if (o.precision == BMFP_SOLVE_MIXED && o.fallback_fp64)
+    {
+      rc = probe_fp32 (sv.get (), s, &sv->fp64_only);
+      if (rc == BMFP_SUCCESS && cudaStreamSynchronize (s) != cudaSuccess)
+        rc = fail (BMFP_ERROR_CUDA, "mixed-precision probe failed");
+      if (rc != BMFP_SUCCESS)
+        return rc;
+    }
   *out = sv.release ();
   return BMFP_SUCCESS;
 }

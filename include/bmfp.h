@@ -297,6 +297,11 @@ typedef struct bmfp_solver_options
                                has not halved within this many iterations (of its start or
                                of its last halving) is stopped there; it is applied if it
                                halved at least once. 0 = never */
+  int residual_replacement; /* 1 (default): FP64 BiCGStab replaces its recursive residual
+                               by the true one near convergence (van der Vorst and Ye,
+                               group update), so stopping on it also meets the tolerance in
+                               b - A x; applies when check_true_residual is 1 (with 0 the
+                               reference's plain recurrences run) */
 } bmfp_solver_options;
 
 typedef struct bmfp_solve_info
@@ -310,6 +315,8 @@ typedef struct bmfp_solve_info
   double true_rel_residual;      /* ||b - A x|| / ||b||, computed in the matrix precision */
   double recursive_rel_residual; /* BiCGStab's own residual at exit */
   double seconds;                /* host wall time of the solve */
+  int replacements;              /* residual replacements (FP64 iterations) */
+  int pad;
 } bmfp_solve_info;
 
 typedef struct bmfp_solver_s *bmfp_solver_t;
@@ -321,7 +328,12 @@ BMFP_API void bmfp_solver_options_init (bmfp_solver_options *opts);
 /* Allocate the Krylov vectors and capture the iteration graph. The matrix must
  * be square and must outlive the solver (for MIXED it must be FP64). This call
  * synchronises the stream; the reference constructor's 80 %-of-memory guard
- * (bicgstab.cu:41-42) becomes BMFP_ERROR_OUT_OF_MEMORY from the allocations. */
+ * (bicgstab.cu:41-42) becomes BMFP_ERROR_OUT_OF_MEMORY from the allocations.
+ * MIXED with fallback_fp64: creation probes the matrix once (the FP32
+ * refinement phase on a seeded right-hand side uniform in [-1, 1)); when
+ * that phase would fall back to FP64, every solve of this solver runs FP64
+ * only (info->used_fp64_fallback = 1, no FP32 iterations). The choice
+ * depends on the matrix alone, never on earlier solves. */
 BMFP_API int bmfp_solver_create (bmfp_solver_t *out, bmfp_matrix_t A, const bmfp_solver_options *opts,
                                  void *stream);
 /* Solve A x = b from x0 = 0. b and x are device vectors of the matrix dtype
@@ -422,16 +434,18 @@ BMFP_API int bmfp_server_destroy (bmfp_server_t s);
  * allocation's implicit synchronisation, plug-ins whose host owns every
  * allocation). The caller passes the matrix (BCSR with bs >= 1, or CSR with
  * bs = 0 and n_block_rows = rows), b and x; every other vector lives in a
- * fixed file-scope device array of about 9.5 MB that each GPU loading the
+ * fixed file-scope device array of about 11.6 MB that each GPU loading the
  * library holds until exit. Limit: n_block_rows * max(bs,1) <= 131072 rows
  * (larger systems get BMFP_ERROR_NOT_SUPPORTED; use bmfp_solver_create).
  * The first call on a device looks up the array's device address; make that
- * first call before any stream capture. All calls share the array: calls
+ * first call before any stream capture, and do not call again after a
+ * cudaDeviceReset of that device. All calls share the array: calls
  * that overlap on the GPU (other threads or streams) race and must be
  * serialised by the caller. Stops on the recursive residual
  * ||r_i|| / ||b|| < tolerance (the reference's rule, gpu/bicgstab.cu:512);
  * *iterations and *rel_residual (that recursive value) may be NULL. Blocks
- * until the solve ends. */
+ * until the solve ends (it synchronises the stream). More than 2^31 - 1
+ * stored values (nnzb * bs^2) get BMFP_ERROR_NOT_SUPPORTED. */
 BMFP_API int bmfp_bicgstab_solve_noalloc (int dtype, int n_block_rows, int bs, int64_t nnzb,
                                           const int *d_row_ptr, const int *d_cols,
                                           const void *d_values, const void *d_b, void *d_x,

@@ -182,3 +182,33 @@ def test_inner_stall_window_keeps_results_and_cuts_fp32_work(lib, cuda):
             bm.Batch([m], "mixed", inner_stall_iterations=-1)
     finally:
         m.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_grids_within_fp64_reach_converge_in_the_batch(lib, cuda, precision):
+    """97x24, 150x38 and 240x60 of the uneven batch (FP64 rounding floors
+    1.7e-11, 3.1e-11, 6.4e-11) end below 1e-10 in b - A x inside a batch:
+    the team solver replaces its recursive residual by the true one near
+    convergence (before, they stopped at 1.0-1.04e-10)."""
+    systems = q4_systems([(97, 24), (150, 38), (240, 60), (40, 10)])
+    xs, infos = run_batch(systems, precision, (4, 512), max_iters=100000)
+    for (rp, c, v, rhs, bs), x, info in zip(systems, xs, infos):
+        K = csr_of(rp, c, v, bs)
+        rel = np.linalg.norm(rhs - K @ x) / np.linalg.norm(rhs)
+        assert info["status"] == bm.SUCCESS and rel < 1e-10, (info, rel)
+        if precision == "fp64" and len(rhs) > 2 * 40 * 10:
+            assert info["replacements"] >= 1, info
+
+
+def test_mixed_result_is_bitwise_the_same_alone_and_in_the_mix(lib, cuda):
+    """Mixed precision in the batch: elasticity systems (FP32 steps fail,
+    FP64 finish) and well-conditioned ones (FP32 refinements) give the same
+    bits and counts alone and inside a mix."""
+    systems = q4_systems(GRIDS[:5]) + [diag_dominant(500, 2, 7), diag_dominant(1200, 2, 8)]
+    xs_mix, inf_mix = run_batch(systems, "mixed", (4, 256), max_iters=50000)
+    for k in (0, 4, 5, 6):
+        xs_one, inf_one = run_batch([systems[k]], "mixed", (4, 256), max_iters=50000)
+        for key in ("iterations", "iterations_fp32", "refinements", "used_fp64_fallback", "status"):
+            assert inf_one[0][key] == inf_mix[k][key], (k, key, inf_one[0], inf_mix[k])
+        assert np.array_equal(xs_one[0].view(np.uint64), xs_mix[k].view(np.uint64)), k
+    assert inf_mix[5]["iterations_fp32"] > 0 and inf_mix[5]["used_fp64_fallback"] == 0

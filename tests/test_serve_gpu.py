@@ -67,7 +67,9 @@ def test_mix_equals_alone_bitwise(problems):
 
 def test_admission_respects_the_budget(problems):
     m, rp, c, v, _ = problems[4]  # 80x20 -> 3200 rows
-    per_request = 256 * 2 * ((m.rows * 8 + 255) // 256) + ((m.rows * 72 + 255) // 256) * 256
+    # b and x, and ten FP64 work vectors (r, rh, p, v, s, t, residual, best x,
+    # snapshot, accumulated update), each slice 256-byte aligned
+    per_request = 256 * 2 * ((m.rows * 8 + 255) // 256) + ((m.rows * 80 + 255) // 256) * 256
     srv = bm.Server("fp64", tol=1e-10, hbm_budget_bytes=int(2.5 * per_request))
     xs = [np.zeros(m.rows) for _ in range(6)]
     bs = [loads(m.rows, k) for k in range(6)]
@@ -156,3 +158,50 @@ def test_finished_request_leaves_before_its_micro_batch(problems):
     big.close()
     assert st["micro_batches"] == 2  # the first request, then the four together
     assert early == 3
+
+
+def _diag_dominant(nbr, seed):
+    rng = np.random.default_rng(seed)
+    rows = [np.unique(np.concatenate([[i], rng.integers(max(0, i - 10), min(nbr, i + 11), 6)])) for i in range(nbr)]
+    rp = np.concatenate([[0], np.cumsum([len(r) for r in rows])]).astype(np.int32)
+    c = np.concatenate(rows).astype(np.int32)
+    v = rng.uniform(-1, 1, c.size * 4)
+    for i in range(nbr):
+        k = rp[i] + int(np.where(rows[i] == i)[0][0])
+        v[k * 4:(k + 1) * 4].reshape(2, 2)[...] += np.eye(2) * (len(rows[i]) * 3.0)
+    return rp, c, v
+
+
+def test_mixed_mix_equals_alone_bitwise(problems):
+    """Mixed precision served: micro-batched requests (elasticity, whose FP32
+    steps fail, and a well-conditioned matrix refined in FP32) and whole-GPU
+    lane requests (the lane's solver decides FP32 or FP64 once, from the
+    matrix) give the same bits alone as in a mix of 14 requests."""
+    rp, c, v = _diag_dominant(1500, 3)
+    good = (bm.Matrix.from_bcsr(rp, c, v, 2), rp, c, v, None)
+    pool = [problems[0], problems[1], problems[4], problems[7], good]  # 80x20 and 100x25 go wide
+    mix = bm.Server("mixed", tol=1e-10, max_batch=4, wide_threshold_rows=3000)
+    reqs = []
+    for k in range(14):
+        m = pool[k % len(pool)][0]
+        b = loads(m.rows, 300 + k)
+        x = np.full(m.rows, np.nan)
+        reqs.append((k, b, x, mix.submit(m, b, x)))
+    results = [(k, b, x, mix.wait(t)) for k, b, x, t in reqs]
+    st = mix.stats()
+    mix.close()
+    assert st["wide_solves"] >= 2 and st["micro_batches"] >= 1
+    refined = 0
+    for k, b, x, info in results[:len(pool)]:
+        m, rp0, c0, v0, _ = pool[k % len(pool)]
+        assert info["status"] == bm.SUCCESS and rel_residual(rp0, c0, v0, b, x) < 1e-10, info
+        refined += info["iterations_fp32"] > 0 and not info["used_fp64_fallback"]
+        alone = bm.Server("mixed", tol=1e-10, wide_threshold_rows=3000)
+        x1 = np.full(m.rows, np.nan)
+        i1 = alone.wait(alone.submit(m, b, x1))
+        alone.close()
+        for key in ("iterations", "iterations_fp32", "used_fp64_fallback"):
+            assert i1[key] == info[key], (k, key, i1, info)
+        assert np.array_equal(x.view(np.uint64), x1.view(np.uint64)), k
+    assert refined >= 1
+    good[0].close()

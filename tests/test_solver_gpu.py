@@ -155,8 +155,9 @@ def test_mixed_precision_ill_conditioned_falls_back_and_converges(lib, cuda):
 def test_reused_solver_gives_the_same_answer_every_time(lib, cuda, precision):
     """A solver object serves many right-hand sides (the server's whole-GPU
     lanes keep one per matrix): nothing of an earlier solve may leak into the
-    next. Mixed precision on this grid ends in the FP64 finish, which once
-    kept counting iterations across solves until the limit stopped it at x = 0."""
+    next. Mixed precision on this grid runs FP64 only (the creation probe
+    finds FP32 steps unable to progress on it), which once kept counting
+    iterations across solves until the limit stopped it at x = 0."""
     rp, c, v, rhs = bm.gen_q4_elasticity(100, 25)
     A = bm.Matrix.from_bcsr(rp, c, v, 2)
     K = bcsr_dense_csr(rp, c, v, 2)
@@ -168,15 +169,48 @@ def test_reused_solver_gives_the_same_answer_every_time(lib, cuda, precision):
         assert info["status"] == bm.SUCCESS, info
         assert info["iterations"] <= 3000
         assert np.linalg.norm(b - K @ x) / np.linalg.norm(b) < 1e-10
-    # From the second solve on a mixed solver knows this matrix needs FP64
-    # and skips the FP32 attempt, so compare the last two.
-    assert np.array_equal(out[2][0].view(np.uint64), out[3][0].view(np.uint64))
-    assert out[2][1]["iterations"] == out[3][1]["iterations"]
+    # The same right-hand side gives the same bits whatever came before.
+    for k in (2, 3):
+        assert np.array_equal(out[0][0].view(np.uint64), out[k][0].view(np.uint64))
+        assert out[0][1]["iterations"] == out[k][1]["iterations"]
     if precision == "mixed":
-        assert out[0][1]["iterations_fp32"] > 0 and out[0][1]["used_fp64_fallback"] == 1
-        assert out[2][1]["iterations_fp32"] == 0 and out[2][1]["used_fp64_fallback"] == 1
-    else:
-        assert np.array_equal(out[0][0].view(np.uint64), out[2][0].view(np.uint64))
+        # decided once per matrix: FP64 only from the first solve on, and then
+        # bit for bit the FP64 solver's answer
+        for _, info in out:
+            assert info["iterations_fp32"] == 0 and info["used_fp64_fallback"] == 1
+        x64, _ = bm.Solver(A, "fp64", tol=1e-10, max_iters=3000).solve_host(rhs)
+        assert np.array_equal(out[0][0].view(np.uint64), x64.view(np.uint64))
+
+
+@pytest.mark.parametrize("grid", [(97, 24), (150, 38), (240, 60)])
+def test_fp64_reaches_the_tolerance_where_fp64_allows(lib, cuda, grid):
+    """Grids of the uneven batch whose FP64 rounding floor u ||A| |x|| / ||b||
+    lies below 1e-10 (1.7e-11, 3.1e-11 and 6.4e-11): the residual replacement
+    keeps BiCGStab's recursive residual on the true one, so the solve ends
+    below 1e-10 in b - A x (plain restarts from the true residual left these
+    at 1.0-1.04e-10)."""
+    nx, ny = grid
+    rp, c, v, rhs = bm.gen_q4_elasticity(nx, ny)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    x, info = bm.Solver(A, "fp64", tol=1e-10, max_iters=50000).solve_host(rhs)
+    K = bcsr_dense_csr(rp, c, v, 2)
+    rel = np.linalg.norm(rhs - K @ x) / np.linalg.norm(rhs)
+    assert info["status"] == bm.SUCCESS and info["true_rel_residual"] < 1e-10, info
+    assert rel < 1e-10, rel
+    assert info["replacements"] >= 1, info
+    floor = 2.0 ** -53 * np.linalg.norm(abs(K) @ abs(x)) / np.linalg.norm(rhs)
+    assert floor < 1e-10
+
+
+def test_replacement_off_keeps_the_plain_recurrences(lib, cuda):
+    """residual_replacement = 0 runs the unmodified recurrences (no
+    replacement happens); the restarts from the true residual remain."""
+    rp, c, v, rhs = bm.gen_q4_elasticity(60, 15)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    x, info = bm.Solver(A, "fp64", tol=1e-10, residual_replacement=0).solve_host(rhs)
+    assert info["replacements"] == 0
+    x1, info1 = bm.Solver(A, "fp64", tol=1e-10).solve_host(rhs)
+    assert info1["replacements"] >= 1 and info1["status"] == bm.SUCCESS, info1
 
 
 def test_zero_rhs_and_iteration_limit(lib, cuda):
