@@ -544,13 +544,12 @@ struct Fp64Result
 };
 
 // FP64 BiCGStab with true-residual restarts: from x = 0 (first) or from the
-// current x with its residual in r64. Restarts continue while each one still
-// lowers the true residual (at most 8); each aims at half the true residual
-// it starts from (a restart asked only for the tolerance again, from just
-// above it, moves x by a hair and the true residual with it). Near FP64's attainable accuracy a restart
-// can leave x worse (asking the recursive residual for less than the
-// tolerance only makes that more likely), so the best iterate is kept (xb)
-// and restored.
+// current x with its residual in r64. Restarts continue while each one at
+// least halves the true residual (at most 8); each aims at half the one it
+// starts from (a restart asked only for the tolerance again, from just above
+// it, moves x by a hair and the true residual with it). Near FP64's
+// attainable accuracy a restart can leave x worse, so the best iterate is
+// kept (xb) and restored.
 template <int OP>
 __device__ Fp64Result fp64_restarted (cg::cluster_group &cl, const TeamSys<double> &S64, const BatchDesc &D,
                                       const BatchParams &P, bool first, int budget, double norm_b, double *r64,
@@ -597,13 +596,16 @@ __device__ Fp64Result fp64_restarted (cg::cluster_group &cl, const TeamSys<doubl
             }
           break;
         }
+      // A restart that did not at least halve the true residual met FP64's
+      // floor (u ||A| |x|| / ||b||): keep its x, stop.
+      const bool halved = rel <= 0.5 * best;
       best = rel;
       f.rel = rel;
       f.status = o.status;
       f.rec = o.rec_rel;
       // A breakdown restarts too (fresh shadow residual); the iteration
       // limit ends the loop.
-      if (rel < P.tol || o.status == 2 || f.iters >= budget || f.restarts >= 8)
+      if (rel < P.tol || o.status == 2 || f.iters >= budget || f.restarts >= 8 || (f.restarts > 0 && !halved))
         break;
       for (int64_t i = ix.elem0; i < D.n; i += ix.elem_stride)
         xb[i] = D.x[i];

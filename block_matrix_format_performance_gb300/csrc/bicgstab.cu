@@ -89,32 +89,52 @@ __device__ __forceinline__ double warp_sum (double v)
   return v;
 }
 
-__device__ __forceinline__ bool is_done (const DevState *st)
+// done and rep_now in one load. Both are written by earlier kernels (done
+// also by block 0 of phases 1, 3 and 5, in cases where every block of that
+// phase takes the same early return anyway), so a plain load suffices.
+__device__ __forceinline__ int2 flags (const DevState *st)
 {
-  // Written by an earlier kernel, or by block 0 of this one in a case where
-  // every block takes the same early return anyway.
-  return *reinterpret_cast<const volatile int *> (&st->done) != 0;
+  return *reinterpret_cast<const int2 *> (&st->done);
 }
 
-// Sum the grid partials of NK kinds in a fixed order (warp 0), broadcast.
+__device__ __forceinline__ bool is_done (const DevState *st) { return flags (st).x != 0; }
+
+// Sum the grid partials of NK kinds in a fixed order, broadcast to the CTA.
+// Every thread loads its share of the partials at once (the grid is a few
+// CTAs per SM, so a handful of loads each), then warps and the warps' totals
+// reduce by butterflies: a few memory round trips instead of one per 32
+// partials, on the path every phase waits for.
 template <int NK>
 __device__ __forceinline__ void sum_parts (const double *part, int grid, const int (&ks)[NK],
                                            double (&out)[NK])
 {
+  __shared__ double sh_w[NK][kWarps];
   __shared__ double sh[NK];
-  if (threadIdx.x < 32)
-    {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double acc[NK];
 #pragma unroll
-      for (int k = 0; k < NK; k++)
-        {
-          double acc = 0.0;
-          for (int i = threadIdx.x; i < grid; i += 32)
-            acc += part[ks[k] * grid + i];
-          acc = warp_sum (acc);
-          if (threadIdx.x == 0)
-            sh[k] = acc;
-        }
+  for (int k = 0; k < NK; k++)
+    acc[k] = 0.0;
+  for (int i = threadIdx.x; i < grid; i += kThreads)
+#pragma unroll
+    for (int k = 0; k < NK; k++)
+      acc[k] += part[ks[k] * grid + i];
+#pragma unroll
+  for (int k = 0; k < NK; k++)
+    {
+      const double s = warp_sum (acc[k]);
+      if (lane == 0)
+        sh_w[k][w] = s;
     }
+  __syncthreads ();
+  if (w == 0)
+#pragma unroll
+    for (int k = 0; k < NK; k++)
+      {
+        const double a = warp_sum (lane < kWarps ? sh_w[k][lane] : 0.0);
+        if (lane == 0)
+          sh[k] = a;
+      }
   __syncthreads ();
 #pragma unroll
   for (int k = 0; k < NK; k++)
@@ -243,20 +263,15 @@ template <typename T> struct EpiReplace
   }
 };
 
-__device__ __forceinline__ bool replacing (const DevState *st)
-{
-  // Written by phase 1 of this iteration, an earlier kernel.
-  return st->rep_now != 0;
-}
-
 // phase 2: v = A q, partial (rh, v); in a replacement iteration r = c - A g
 // with partials (rh, r), (r, r) instead (A g lands in t, free until phase 4).
 template <typename T, class Op>
 __global__ void __launch_bounds__ (kThreads) phase_v (Args<T> a)
 {
-  if (is_done (a.st))
+  const int2 f = flags (a.st);
+  if (f.x)
     return;
-  if (replacing (a.st))
+  if (f.y)
     {
       EpiReplace<T> e{ static_cast<const T *> (a.st->c), a.r, a.rh };
       Op::run (a, a.g, a.t, e);
@@ -276,7 +291,8 @@ __global__ void __launch_bounds__ (kThreads) phase_v (Args<T> a)
 template <typename T, class Op>
 __global__ void __launch_bounds__ (kThreads) phase_t (Args<T> a)
 {
-  if (is_done (a.st) || replacing (a.st))
+  const int2 f = flags (a.st);
+  if (f.x || f.y)
     return;
   EpiTS<T> e{ a.s };
   Op::run (a, a.z, a.t, e);
@@ -495,7 +511,8 @@ template <typename T, bool PRE>
 __global__ void __launch_bounds__ (kThreads) phase_s (Args<T> a)
 {
   DevState *st = a.st;
-  if (is_done (st) || replacing (st))
+  const int2 f = flags (st);
+  if (f.x || f.y)
     return;
   double s[1];
   const int ks[1] = { kRhV };
@@ -560,9 +577,10 @@ template <typename T, bool PRE>
 __global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
 {
   DevState *st = a.st;
-  if (is_done (st))
+  const int2 f = flags (st);
+  if (f.x)
     return;
-  if (replacing (st))
+  if (f.y)
     {
       // r, (rh, r) and (r, r) came from phase 2; nothing else moves.
       if (blockIdx.x == 0 && threadIdx.x == 0)

@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cstddef>
 #include <cstdint>
 
 namespace bmfp
@@ -41,11 +42,13 @@ struct DevState
   // old values), phase 5 flips dslot.
   double dev[2], dev0[2], nr_prev[2];
   const void *c;   // right-hand side of the run (b, or a restart's residual)
+  // done and rep_now side by side (8-byte aligned): every phase reads both
+  // with one load at its start.
+  int done;        // set by phase 1; every kernel returns early once set
+  int rep_now;     // phase 1 chose to replace r this iteration (read by phases 2-5)
   int iter;        // iterations completed (phase 5)
   int max_iter;
-  int done;        // set by phase 1; every kernel returns early once set
   int status;      // 0 running, 1 converged, 2 iteration limit, 3 breakdown
-  int rep_now;     // phase 1 chose to replace r this iteration (read by phases 2-5)
   int rep_done;    // the iteration phase 5 just closed was a replacement (read by phase 1)
   int replacements;
   int dslot;
@@ -55,6 +58,9 @@ struct DevState
 // 1e-3 measured best on the Q4 elasticity family: every grid up to 400x100
 // ends below 1e-10 in b - A x with one to three replacements).
 constexpr double kReplaceThreshold = 1e-3;
+
+static_assert (offsetof (DevState, done) % 8 == 0 && offsetof (DevState, rep_now) == offsetof (DevState, done) + 4,
+               "done and rep_now must form one aligned 8-byte word");
 
 enum
 {
