@@ -4,6 +4,8 @@
  * x86 and Arm hosts produce identical bits (no fused multiply-add contraction),
  * matching the reference's own x86 host build, which has no FMA either.
  */
+/* POSIX barriers (the threaded BiCGStab) under -std=c11 */
+#define _POSIX_C_SOURCE 200809L
 #include "oracle.h"
 
 #include <math.h>
@@ -453,4 +455,384 @@ int orc_bicgstab_f64 (int n, const int *row_ptr, const int *cols, const double *
     }
   free (mem);
   return status;
+}
+
+/* ---------------------------------------------- band generator (C) --- */
+/* The seeded random-band workload of the block-size sweep, restated from
+ * its specification (the same as oracle.py's numpy gen_band_bcsr, which the
+ * tests pin to the product's generator): block row i takes min(k, W)
+ * distinct block columns from [max(0, i-h), min(nbr-1, i+h)] (W wide) by a
+ * partial Fisher-Yates shuffle on a per-row SplitMix64 stream (stream 0),
+ * sorted; its k*bs*bs values U[-1, 1) come in storage order from stream 1.
+ * No reference counterpart: the reference generates only contiguous bands
+ * (gen_n_diag_bcsr). The CSR form expands the blocks directly (the CPU
+ * baseline's input, common/matrix_converters.h:88-117 layout), threaded
+ * over block rows, whose streams are independent. */
+
+static uint64_t orc_mix64 (uint64_t z)
+{
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+static uint64_t orc_next (uint64_t *state)
+{
+  *state += 0x9E3779B97F4A7C15ull;
+  return orc_mix64 (*state);
+}
+
+static uint64_t orc_row_state (uint64_t seed, uint64_t stream, uint64_t row)
+{
+  uint64_t s = row * 0x9E3779B97F4A7C15ull + (seed * 0xD1B54A32D192ED03ull + stream * 0x8CB92BA72F3D8DD7ull);
+  return orc_next (&s);
+}
+
+static double orc_pm1 (uint64_t z) { return (double) (z >> 11) * (2.0 / 9007199254740992.0) - 1.0; }
+
+static int orc_band_width (int i, int nbr, int half, int *lo)
+{
+  *lo = i - half > 0 ? i - half : 0;
+  const int hi = i + half < nbr - 1 ? i + half : nbr - 1;
+  return hi - *lo + 1;
+}
+
+int orc_band_blocks (int nbr, int bpr, int half, int i)
+{
+  int lo;
+  const int w = orc_band_width (i, nbr, half, &lo);
+  return bpr < w ? bpr : w;
+}
+
+/* The sorted block columns of block row i (k of them) into out. */
+static void orc_band_cols (int nbr, int bpr, int half, uint64_t seed, int i, int *perm, int *out)
+{
+  int lo;
+  const int w = orc_band_width (i, nbr, half, &lo);
+  const int k = bpr < w ? bpr : w;
+  for (int j = 0; j < w; j++)
+    perm[j] = j;
+  uint64_t st = orc_row_state (seed, 0, (uint64_t) i);
+  for (int j = 0; j < k; j++)
+    {
+      const uint64_t z = orc_next (&st);
+      const int pick = j + (int) (z % (uint64_t) (w - j));
+      const int a = perm[j];
+      perm[j] = perm[pick];
+      perm[pick] = a;
+    }
+  for (int j = 0; j < k; j++)
+    out[j] = perm[j] + lo;
+  qsort (out, (size_t) k, sizeof (int), orc_cmp_int);
+}
+
+typedef struct
+{
+  int nbr, bpr, half, bs, is_f64, csr, begin, end;
+  uint64_t seed;
+  const int64_t *row_ptr; /* block-row offsets (BCSR) or scalar-row offsets (CSR) */
+  int *cols;
+  void *vals;
+} orc_band_task;
+
+static void *orc_band_worker (void *arg)
+{
+  const orc_band_task *t = (const orc_band_task *) arg;
+  const int bs = t->bs, e = bs * bs;
+  int *perm = (int *) malloc (sizeof (int) * (size_t) (2 * t->half + 1));
+  int *bc = (int *) malloc (sizeof (int) * (size_t) (t->bpr > 0 ? t->bpr : 1));
+  double *blk = (double *) malloc (sizeof (double) * (size_t) t->bpr * e + 1);
+  for (int i = t->begin; i < t->end; i++)
+    {
+      const int k = orc_band_blocks (t->nbr, t->bpr, t->half, i);
+      orc_band_cols (t->nbr, t->bpr, t->half, t->seed, i, perm, bc);
+      uint64_t vs = orc_row_state (t->seed, 1, (uint64_t) i);
+      for (int j = 0; j < k * e; j++)
+        blk[j] = orc_pm1 (orc_next (&vs));
+      if (!t->csr)
+        {
+          const int64_t b0 = t->row_ptr[i];
+          for (int b = 0; b < k; b++)
+            t->cols[b0 + b] = bc[b];
+          for (int j = 0; j < k * e; j++)
+            {
+              if (t->is_f64)
+                ((double *) t->vals)[b0 * e + j] = blk[j];
+              else
+                ((float *) t->vals)[b0 * e + j] = (float) blk[j];
+            }
+          continue;
+        }
+      for (int r = 0; r < bs; r++)
+        {
+          int64_t o = t->row_ptr[(int64_t) i * bs + r];
+          for (int b = 0; b < k; b++)
+            for (int c = 0; c < bs; c++, o++)
+              {
+                t->cols[o] = bc[b] * bs + c;
+                const double v = blk[(size_t) b * e + (size_t) r * bs + c];
+                if (t->is_f64)
+                  ((double *) t->vals)[o] = v;
+                else
+                  ((float *) t->vals)[o] = (float) v;
+              }
+        }
+    }
+  free (perm);
+  free (bc);
+  free (blk);
+  return NULL;
+}
+
+/* row_ptr: the caller's offsets (int64, from orc_band_blocks); cols and
+ * vals: BCSR (csr = 0) or CSR (csr = 1). */
+void orc_gen_band (int nbr, int bpr, int half, int bs, uint64_t seed, int is_f64, int csr,
+                   const int64_t *row_ptr, int *cols, void *vals, int threads)
+{
+  if (threads < 1)
+    threads = 1;
+  if (threads > 256)
+    threads = 256;
+  pthread_t tid[256];
+  orc_band_task task[256];
+  for (int t = 0; t < threads; t++)
+    {
+      orc_band_task *k = &task[t];
+      k->nbr = nbr;
+      k->bpr = bpr;
+      k->half = half;
+      k->bs = bs;
+      k->is_f64 = is_f64;
+      k->csr = csr;
+      k->seed = seed;
+      k->row_ptr = row_ptr;
+      k->cols = cols;
+      k->vals = vals;
+      k->begin = (int) ((int64_t) nbr * t / threads);
+      k->end = (int) ((int64_t) nbr * (t + 1) / threads);
+      if (threads > 1)
+        pthread_create (&tid[t], NULL, orc_band_worker, k);
+      else
+        orc_band_worker (k);
+    }
+  if (threads > 1)
+    for (int t = 0; t < threads; t++)
+      pthread_join (tid[t], NULL);
+}
+
+/* x_i = U[-1, 1) of the row state (seed, stream, i). */
+void orc_gen_uniform_vector (int64_t n, uint64_t seed, uint64_t stream, int is_f64, void *out)
+{
+  for (int64_t i = 0; i < n; i++)
+    {
+      const double v = orc_pm1 (orc_row_state (seed, stream, (uint64_t) i));
+      if (is_f64)
+        ((double *) out)[i] = v;
+      else
+        ((float *) out)[i] = (float) v;
+    }
+}
+
+/* ------------------------------------------- threaded BiCGStab (CPU) --- */
+/* The recurrences of orc_bicgstab_f64 (gpu/bicgstab.cu:426-513, last
+ * iterate returned) on `threads` host threads: each owns a contiguous range
+ * of rows for every vector update and product; dot products are per-thread
+ * partials summed in thread order by every thread. The CPU solve baseline
+ * on all host cores; orc_bicgstab_f64 is the single-thread one (and this
+ * function with one thread reproduces it bit for bit). */
+
+typedef struct
+{
+  int n, threads, max_iterations, use_precond;
+  const int *row_ptr, *cols;
+  const double *vals, *b;
+  double *x, *mem, eps, norm_b;
+  double *part; /* threads x 4 partial sums */
+  pthread_barrier_t *bar;
+  int status, iters;
+  double rel;
+} orc_bicg_shared;
+
+typedef struct
+{
+  orc_bicg_shared *S;
+  int t;
+} orc_bicg_arg;
+
+static double orc_sum_part (const orc_bicg_shared *S, int k)
+{
+  double s = 0.0;
+  for (int t = 0; t < S->threads; t++)
+    s += S->part[t * 4 + k];
+  return s;
+}
+
+static void *orc_bicg_worker (void *arg)
+{
+  orc_bicg_shared *S = ((orc_bicg_arg *) arg)->S;
+  const int t = ((orc_bicg_arg *) arg)->t, n = S->n;
+  const int lo = (int) ((int64_t) n * t / S->threads), hi = (int) ((int64_t) n * (t + 1) / S->threads);
+  double *r = S->mem, *rh = r + n, *p = r + 2 * (size_t) n, *v = r + 3 * (size_t) n, *h = r + 4 * (size_t) n;
+  double *s = r + 5 * (size_t) n, *tv = r + 6 * (size_t) n, *P = r + 7 * (size_t) n, *q = r + 8 * (size_t) n;
+  double *z = r + 9 * (size_t) n, *x = S->x;
+  double *my = S->part + t * 4;
+  for (int row = lo; row < hi; row++)
+    {
+      P[row] = 1.0;
+      if (S->use_precond)
+        for (int e = S->row_ptr[row]; e < S->row_ptr[row + 1]; e++)
+          if (S->cols[e] == row)
+            {
+              P[row] = fabs (S->vals[e]) < 1e-20 ? 1.0 : 1.0 / S->vals[e];
+              break;
+            }
+      x[row] = 0.0;
+      r[row] = rh[row] = S->b[row];
+      p[row] = v[row] = 0.0;
+    }
+  double rho_prev = 1.0, omega_prev = 1.0, alpha = 1.0;
+  int status = 1, iters = 0;
+  double rel = S->norm_b > 0 ? 1.0 : 0.0;
+  for (int it = 0; it < S->max_iterations && S->norm_b > 0; it++)
+    {
+      double a = 0.0;
+      for (int i = lo; i < hi; i++)
+        a += rh[i] * r[i];
+      my[0] = a;
+      pthread_barrier_wait (S->bar);
+      const double rho = orc_sum_part (S, 0);
+      if (rho == 0.0)
+        {
+          status = 2;
+          break;
+        }
+      const double beta = rho / rho_prev * alpha / omega_prev;
+      for (int i = lo; i < hi; i++)
+        {
+          p[i] = r[i] + beta * (p[i] - omega_prev * v[i]);
+          q[i] = S->use_precond ? P[i] * p[i] : p[i];
+        }
+      pthread_barrier_wait (S->bar);
+      a = 0.0;
+      for (int row = lo; row < hi; row++)
+        {
+          double dot = 0.0;
+          for (int e = S->row_ptr[row]; e < S->row_ptr[row + 1]; e++)
+            dot += S->vals[e] * q[S->cols[e]];
+          v[row] = dot;
+          a += rh[row] * dot;
+        }
+      my[1] = a;
+      pthread_barrier_wait (S->bar);
+      const double rh_v = orc_sum_part (S, 1);
+      if (rh_v == 0.0)
+        {
+          status = 2;
+          break;
+        }
+      alpha = rho / rh_v;
+      for (int i = lo; i < hi; i++)
+        {
+          h[i] = x[i] + alpha * q[i];
+          s[i] = r[i] - alpha * v[i];
+          z[i] = S->use_precond ? P[i] * s[i] : s[i];
+        }
+      pthread_barrier_wait (S->bar);
+      double ts = 0.0, tt = 0.0;
+      for (int row = lo; row < hi; row++)
+        {
+          double dot = 0.0;
+          for (int e = S->row_ptr[row]; e < S->row_ptr[row + 1]; e++)
+            dot += S->vals[e] * z[S->cols[e]];
+          tv[row] = dot;
+          ts += dot * s[row];
+          tt += dot * dot;
+        }
+      my[2] = ts;
+      my[3] = tt;
+      pthread_barrier_wait (S->bar);
+      const double tsum = orc_sum_part (S, 2), ttsum = orc_sum_part (S, 3);
+      if (ttsum == 0.0)
+        {
+          status = 2;
+          break;
+        }
+      const double omega = tsum / ttsum;
+      a = 0.0;
+      for (int i = lo; i < hi; i++)
+        {
+          r[i] = s[i] - omega * tv[i];
+          x[i] = h[i] + omega * z[i];
+          a += r[i] * r[i];
+        }
+      /* part 1 was last read after the (rh, v) barrier, two barriers ago:
+       * it carries the (r, r) sum now */
+      my[1] = a;
+      pthread_barrier_wait (S->bar);
+      iters = it + 1;
+      rel = sqrt (orc_sum_part (S, 1)) / S->norm_b;
+      if (rel < S->eps)
+        {
+          status = 0;
+          break;
+        }
+      rho_prev = rho;
+      omega_prev = omega;
+    }
+  if (t == 0)
+    {
+      S->status = S->norm_b > 0 ? status : 0;
+      S->iters = iters;
+      S->rel = rel;
+    }
+  return NULL;
+}
+
+int orc_bicgstab_mt_f64 (int n, const int *row_ptr, const int *cols, const double *vals, const double *b,
+                         double *x, double eps, int max_iterations, int use_precond, int threads, int *iters,
+                         double *rel_res)
+{
+  if (threads < 1)
+    threads = 1;
+  if (threads > 256)
+    threads = 256;
+  orc_bicg_shared S;
+  memset (&S, 0, sizeof S);
+  S.n = n;
+  S.threads = threads;
+  S.max_iterations = max_iterations;
+  S.use_precond = use_precond;
+  S.row_ptr = row_ptr;
+  S.cols = cols;
+  S.vals = vals;
+  S.b = b;
+  S.x = x;
+  S.eps = eps;
+  S.mem = (double *) calloc ((size_t) n * 10, sizeof (double));
+  S.part = (double *) calloc ((size_t) threads * 4, sizeof (double));
+  double nb = 0.0;
+  for (int i = 0; i < n; i++)
+    nb += b[i] * b[i];
+  S.norm_b = sqrt (nb);
+  pthread_barrier_t bar;
+  pthread_barrier_init (&bar, NULL, (unsigned) threads);
+  S.bar = &bar;
+  pthread_t tid[256];
+  orc_bicg_arg args[256];
+  for (int t = 0; t < threads; t++)
+    {
+      args[t].S = &S;
+      args[t].t = t;
+      if (t > 0)
+        pthread_create (&tid[t], NULL, orc_bicg_worker, &args[t]);
+    }
+  orc_bicg_worker (&args[0]);
+  for (int t = 1; t < threads; t++)
+    pthread_join (tid[t], NULL);
+  pthread_barrier_destroy (&bar);
+  free (S.mem);
+  free (S.part);
+  *iters = S.iters;
+  *rel_res = S.rel;
+  return S.status;
 }

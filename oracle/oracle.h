@@ -94,6 +94,21 @@ int orc_bicgstab_f64 (int n, const int *row_ptr, const int *cols, const double *
                       const double *b, double *x, double eps, int max_iterations,
                       int use_precond, int *iters, double *rel_res);
 
+/* Seeded random-band generator (the block-size sweep's workload, restated
+ * from its specification): orc_band_blocks gives block row i's block count;
+ * orc_gen_band fills BCSR (csr = 0: row_ptr = block-row offsets) or CSR
+ * (csr = 1: row_ptr = scalar-row offsets) columns and values (is_f64: double,
+ * else float), on `threads` host threads. */
+int orc_band_blocks (int nbr, int bpr, int half, int i);
+void orc_gen_band (int nbr, int bpr, int half, int bs, uint64_t seed, int is_f64, int csr,
+                   const int64_t *row_ptr, int *cols, void *vals, int threads);
+void orc_gen_uniform_vector (int64_t n, uint64_t seed, uint64_t stream, int is_f64, void *out);
+/* orc_bicgstab_f64's recurrences on `threads` host threads (rows split in
+ * contiguous ranges, dot products summed in thread order). */
+int orc_bicgstab_mt_f64 (int n, const int *row_ptr, const int *cols, const double *vals, const double *b,
+                         double *x, double eps, int max_iterations, int use_precond, int threads, int *iters,
+                         double *rel_res);
+
 #ifdef __cplusplus
 }
 #endif

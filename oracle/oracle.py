@@ -59,6 +59,17 @@ def lib():
                                        ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                        ctypes.POINTER(ctypes.c_double)]
         L.orc_bicgstab_f64.restype = ctypes.c_int
+        L.orc_bicgstab_mt_f64.argtypes = [ctypes.c_int, _i32p, _i32p, _f64p, _f64p, _f64p, ctypes.c_double,
+                                          ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                          ctypes.POINTER(ctypes.c_double)]
+        L.orc_bicgstab_mt_f64.restype = ctypes.c_int
+        L.orc_band_blocks.argtypes = [ctypes.c_int] * 4
+        L.orc_band_blocks.restype = ctypes.c_int
+        L.orc_gen_band.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
+                                   ctypes.c_int, ctypes.c_int, np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS"),
+                                   _i32p, ctypes.c_void_p, ctypes.c_int]
+        L.orc_gen_uniform_vector.argtypes = [ctypes.c_int64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
+                                             ctypes.c_void_p]
         _LIB = L
     return _LIB
 
@@ -78,13 +89,15 @@ def _c(a, dtype):
 
 # ------------------------------------------------------------------- SpMV ---
 
-def csr_spmv(row_ptr, cols, vals, x, threads=1):
-    """y = A x over CSR in the reference loop order (main.cpp:36-45)."""
+def csr_spmv(row_ptr, cols, vals, x, threads=1, out=None):
+    """y = A x over CSR in the reference loop order (main.cpp:36-45); `out`
+    (n elements of the value type) receives y when given."""
     vals = np.ascontiguousarray(vals)
     t = _tag(vals.dtype)
     row_ptr = _c(row_ptr, np.int32)
     n = row_ptr.size - 1
-    y = np.zeros(n, dtype=vals.dtype)
+    y = np.zeros(n, dtype=vals.dtype) if out is None else out
+    assert y.dtype == vals.dtype and y.size == n and y.flags.c_contiguous
     x = _c(x, vals.dtype)
     if threads > 1:
         getattr(lib(), f"orc_csr_spmv_mt_{t}")(n, row_ptr, _c(cols, np.int32), vals, x, y, threads)
@@ -197,6 +210,19 @@ def bicgstab(row_ptr, cols, vals, b, eps, max_iterations, use_precond=False):
 _M64 = (1 << 64) - 1
 
 
+def bicgstab_mt(row_ptr, cols, vals, b, eps, max_iterations, threads, use_precond=False):
+    """bicgstab's recurrences on `threads` host threads (the CPU solve
+    baseline on all cores). Returns (x, status, iterations, rel residual)."""
+    b = _c(b, np.float64)
+    x = np.zeros_like(b)
+    it = ctypes.c_int(0)
+    rr = ctypes.c_double(0.0)
+    st = lib().orc_bicgstab_mt_f64(b.size, _c(row_ptr, np.int32), _c(cols, np.int32), _c(vals, np.float64), b, x,
+                                   eps, max_iterations, int(use_precond), threads, ctypes.byref(it),
+                                   ctypes.byref(rr))
+    return x, st, it.value, rr.value
+
+
 def _splitmix64(state):
     """SplitMix64 (Steele, Lea, Flood 2014) over uint64 numpy arrays."""
     with np.errstate(over="ignore"):
@@ -272,6 +298,42 @@ def gen_uniform_vector(n, seed, stream, dtype=np.float64):
     """x_i = U[-1,1) from splitmix64 of (seed, stream, i)."""
     z = _row_states(seed, stream, np.arange(n, dtype=np.int64))
     return _uniform_pm1(z).astype(dtype)
+
+
+def band_block_counts(n_block_rows, blocks_per_row, half_band):
+    """Blocks per block row of the seeded band workload: min(k, band width)."""
+    rows = np.arange(n_block_rows, dtype=np.int64)
+    w = np.minimum(n_block_rows - 1, rows + half_band) - np.maximum(0, rows - half_band) + 1
+    return np.minimum(blocks_per_row, w)
+
+
+def gen_band_c(n_block_rows, blocks_per_row, half_band, bs, seed, dtype=np.float64, csr=False, threads=1):
+    """The band generator of oracle.c (the specification of gen_band_bcsr
+    above, in C, threaded over block rows): BCSR (row_ptr, cols, vals) or,
+    with csr=True, its CSR expansion (the reference CPU loop's input) without
+    the BCSR intermediate."""
+    k = band_block_counts(n_block_rows, blocks_per_row, half_band)
+    if csr:
+        rp64 = np.zeros(n_block_rows * bs + 1, np.int64)
+        np.cumsum(np.repeat(k * bs, bs), out=rp64[1:])
+    else:
+        rp64 = np.zeros(n_block_rows + 1, np.int64)
+        np.cumsum(k, out=rp64[1:])
+    if rp64[-1] > np.iinfo(np.int32).max:
+        raise ValueError("offsets exceed 32 bits")
+    # CSR: rp64[-1] scalar entries; BCSR: rp64[-1] blocks of bs*bs values
+    cols = np.empty(int(rp64[-1]), np.int32)
+    vals = np.empty(int(rp64[-1]) * (1 if csr else bs * bs), np.dtype(dtype))
+    lib().orc_gen_band(n_block_rows, blocks_per_row, half_band, bs, seed, int(np.dtype(dtype) == np.float64),
+                       int(csr), rp64, cols, vals.ctypes.data, threads)
+    return rp64.astype(np.int32), cols, vals
+
+
+def gen_uniform_vector_c(n, seed, stream, dtype=np.float64):
+    """gen_uniform_vector in C."""
+    out = np.empty(n, np.dtype(dtype))
+    lib().orc_gen_uniform_vector(n, seed, stream, int(np.dtype(dtype) == np.float64), out.ctypes.data)
+    return out
 
 
 def q4_element_stiffness(E=1.0, nu=0.3, t=1.0, hx=1.0, hy=1.0):
