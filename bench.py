@@ -73,6 +73,14 @@ def parse_args():
     ap.add_argument("--no-ref-variants", action="store_true",
                     help="skip timing the reference's own kernels on the sweep matrices")
     ap.add_argument("--no-solver", action="store_true", help="skip the batched-solve part of the line")
+    ap.add_argument("--no-fem", action="store_true", help="skip the FEM solves (configs 0 and 2) of the line")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served stream (config 4) of the line")
+    ap.add_argument("--serve-requests", type=int, default=5000, help="line: requests of the served stream")
+    ap.add_argument("--sustained-requests", type=int, default=None,
+                    help="line: requests of the sustained-rate stream (default: --serve-requests)")
+    ap.add_argument("--serve-precisions", default="fp64,mixed", help="line: server precisions at the stated rate")
+    ap.add_argument("--sustained-factor", type=float, default=0.7,
+                    help="line: sustained rate as a fraction of the first server's throughput at the stated rate")
     ap.add_argument("--no-autotune", action="store_true",
                     help="use the autotuner's GB300 picks (built-in table, column owner at FP64 bs 16/32) "
                          "instead of timing candidates")
@@ -493,9 +501,10 @@ def run_ours(args):
     e2e_s = max_over_ranks(e2e_s, dist, "cuda")
     e2e_value = replica_value(total_bytes, world, e2e_s)
 
+    del pinned, h_y
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(cases, nbr=nbr)
+        cpu = cpu_baseline(sizes, dtypes, nbr=nbr)
 
     # Solver side of the metric: the uneven batch of elasticity systems at
     # 1e-10, batched FP64 and mixed against the plain FP64 per-request solver.
@@ -506,6 +515,21 @@ def run_ours(args):
         torch.cuda.empty_cache()
         solves = measure_batch(["fp64", "mixed"], 1e-10, 100000, 2)
         solves_shifted = measure_batch(["fp64", "mixed"], 1e-10, 100000, 2, shift=1e-3)
+    # The FEM workloads of configs 0 and 2, the live cost of one solver
+    # iteration against its floors, and the served stream of config 4.
+    fem = None
+    if not args.no_fem:
+        t0 = time.perf_counter()
+        fem = {"config0_200x50": fem_small(flush, stream),
+               "iteration_roofline": [iteration_roofline(g, hbm, fp64_gflops) for g in ((1000, 250), (2000, 500))],
+               "config2_2000x500": fem_large()}
+        fem["wall_s"] = round(time.perf_counter() - t0, 1)
+    serve = None
+    if not args.no_serve:
+        t0 = time.perf_counter()
+        serve = serve_suite(args.serve_requests, args.rate, args.serve_precisions.split(","), args.sustained_factor,
+                            sustained_requests=args.sustained_requests)
+        serve["wall_s"] = round(time.perf_counter() - t0, 1)
 
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world,
@@ -538,6 +562,10 @@ def run_ours(args):
                                       "bs 2, 1e-10 true relative residual", **solves}
         line["solves_implicit_step"] = {"workload": "the same 256 grids with K + 1e-3 I (implicit time step, unit "
                                                     "lumped mass): FP32 inner solves converge", **solves_shifted}
+    if fem is not None:
+        line["fem"] = fem
+    if serve is not None:
+        line["serve"] = serve
     if rank == 0:
         print(json_line(line), flush=True)
     if dist:
@@ -546,77 +574,123 @@ def run_ours(args):
 
 # ------------------------------------------------------------- CPU sides
 
-def cpu_sample(bm, cs, rows):
-    """First `rows` block rows of a case as CSR (the reference's CPU input)."""
-    rp = cs["rp"][:rows + 1].copy()
-    nnzb = int(rp[-1])
-    bs = cs["bs"]
-    crp, cc, cv = bm.bcsr_to_csr(rp, cs["c"][:nnzb], cs["v"][:nnzb * bs * bs], bs)
-    return crp, cc, cv, case_bytes(bs, cs["tag"], nnzb, rows)
+# Written before every CPU product, outside the timing: more than twice the
+# largest last-level cache of the hosts this runs on (Grace: 114 MB), so
+# every product streams its matrix from DRAM, like the L2-flushed GPU side.
+CPU_FLUSH_BYTES = 256 << 20
 
 
-def cpu_baseline(cases, rows=20_000, reps=3, nbr=NBR):
-    """Oracle restatement of main.cpp:36-45 (one thread) on a bounded sample."""
+class CpuFlush:
+    """Evicts the host's last-level cache by writing a buffer larger than it."""
+
+    def __init__(self, nbytes=CPU_FLUSH_BYTES):
+        self.buf = np.zeros(nbytes // 8, np.float64)
+        self.k = 0.0
+
+    def __call__(self):
+        self.k += 1.0
+        self.buf.fill(self.k)
+
+
+def cpu_sweep(sizes, dtypes, nbr, threads, steps, warmup):
+    """The reference CPU loop (main.cpp:36-45, restated in oracle.c) over the
+    FULL sweep matrices as CSR, generated by the oracle's C restatement of the
+    band generator (no product code), one matrix at a time: `warmup` untimed
+    and `steps` timed products each, the host LLC flushed before every
+    product (outside the timing). Bytes are the workload's algorithmic bytes
+    (the BCSR formula, as on the GPU side). Returns (bytes per step, seconds
+    per step, {case: GB/s})."""
+    from oracle import oracle as orc
+    orc.build()
+    flush = CpuFlush()
+    gen_threads = os.cpu_count() or 1
+    tot_b, tot_s, per = 0, 0.0, {}
+    for tag in dtypes:
+        for bs in sizes:
+            crp, cc, cv = orc.gen_band_c(nbr, BPR, HALF_BAND, bs, SEED, np_dt(tag), csr=True, threads=gen_threads)
+            x = orc.gen_uniform_vector_c(nbr * bs, SEED, X_STREAM, np_dt(tag))
+            y = np.zeros_like(x)
+            nb = case_bytes(bs, tag, cv.size // (bs * bs), nbr)
+            for _ in range(warmup):
+                flush()
+                orc.csr_spmv(crp, cc, cv, x, threads=threads, out=y)
+            t = 0.0
+            for _ in range(steps):
+                flush()
+                t0 = time.perf_counter()
+                orc.csr_spmv(crp, cc, cv, x, threads=threads, out=y)
+                t += time.perf_counter() - t0
+            per[f"bs{bs}_{tag}"] = round(nb * steps / t / 1e9, 2)
+            tot_b += nb
+            tot_s += t / steps
+            del crp, cc, cv
+    return tot_b, tot_s, per
+
+
+def cpu_baseline(sizes, dtypes, nbr=NBR, steps=2):
+    """Oracle restatement of main.cpp:36-45 on one core (as the reference
+    times it) over the full sweep."""
+    b, sec, per = cpu_sweep(sizes, dtypes, nbr, 1, steps, 0)
+    return {"value": round(b / sec / 1e9, 2), "unit": "GB/s", "cores": 1, "kind": "port",
+            "sample": f"the full {nbr}-block-row sweep matrices as CSR ({len(sizes) * len(dtypes)} cases), {steps} "
+                      "products each, the host LLC flushed (256 MB write) before every product; the reference "
+                      "CPU loop main.cpp:36-45 restated in C (oracle/oracle.c, -O2, one thread); inputs from the "
+                      "oracle's C band generator", "per_case_gbs": per}
+
+
+def cpu_solve(grid, threads, max_iterations=100000, tol=1e-10):
+    """The reference BiCGStab recurrences (gpu/bicgstab.cu:426-513, restated
+    in oracle.c, last iterate returned) on the host: FP64, no
+    preconditioner, on `threads` host threads (1 = orc_bicgstab_f64, the
+    reference's single-threaded form). Returns the iterations, seconds and
+    the true relative residual."""
     import block_matrix_format_performance_gb300 as bm
     from oracle import oracle as orc
-    tot_b, tot_s = 0, 0.0
-    for cs in cases:
-        crp, cc, cv, b = cpu_sample(bm, cs, rows)
-        x = cs["x"]
-        orc.csr_spmv(crp, cc, cv, x)
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            orc.csr_spmv(crp, cc, cv, x)
-        tot_s += (time.perf_counter() - t0) / reps
-        tot_b += b
-    return {"value": round(tot_b / tot_s / 1e9, 2), "unit": "GB/s", "cores": 1, "kind": "port",
-            "sample": f"first {rows} of {nbr} block rows of each of the {len(cases)} sweep matrices, CSR, "
-                      f"{reps} passes; the reference CPU loop main.cpp:36-45 restated in C (-O2)"}
+    nx, ny = grid
+    rp, c, v, rhs = bm.gen_q4_elasticity(nx, ny)  # host-side generator (the workload's input)
+    crp, cc, cv = orc.bcsr_to_csr(rp, c, v, 2)
+    del rp, c, v
+    t0 = time.perf_counter()
+    if threads == 1:
+        x, st, it, rel = orc.bicgstab(crp, cc, cv, rhs, tol, max_iterations)
+    else:
+        x, st, it, rel = orc.bicgstab_mt(crp, cc, cv, rhs, tol, max_iterations, threads)
+    sec = time.perf_counter() - t0
+    y = orc.csr_spmv(crp, cc, cv, x, threads=max(1, threads))
+    true_rel = float(np.linalg.norm(rhs - y) / np.linalg.norm(rhs))
+    return {"threads": threads, "iterations": it, "seconds": round(sec, 4), "s_per_iteration": sec / max(it, 1),
+            "status": st, "recursive_rel": rel, "true_rel": true_rel}
 
 
 def run_reference(args):
+    """The reference's CPU path on the host cores: the CSR loop of
+    main.cpp:36-45 (restated in oracle.c: the reference's main.cpp needs the
+    absent fmt and cuda_jit submodules) on all host threads over the full
+    sweep matrices, generated by the oracle (no product code is imported)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    import block_matrix_format_performance_gb300 as bm
-    from block_matrix_format_performance_gb300 import build as B
-    from oracle import oracle as orc
-    B.build()
-    orc.build()
     threads = os.cpu_count() or 1
     sizes = [int(s) for s in args.sizes.split(",")]
     dtypes = args.dtypes.split(",")
-    rows = 25_000
-    samples, tot_b = [], 0
-    for tag in dtypes:
-        for bs in sizes:
-            r = rows if bs < 32 else rows // 2
-            rp, c, v = bm.gen_band_bcsr(NBR, BPR, HALF_BAND, bs, SEED, np_dt(tag))
-            x = bm.gen_uniform_vector(NBR * bs, SEED, X_STREAM, np_dt(tag))
-            crp, cc, cv, b = cpu_sample(bm, {"rp": rp, "c": c, "v": v, "bs": bs, "tag": tag}, r)
-            del rp, c, v
-            samples.append((crp, cc, cv, x))
-            tot_b += b
-    for _ in range(args.warmup):
-        for s in samples:
-            orc.csr_spmv(*s, threads=threads)
+    steps = max(1, args.steps)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        for s in samples:
-            orc.csr_spmv(*s, threads=threads)
-    dt = (time.perf_counter() - t0) / args.steps
-    value = tot_b / dt / 1e9
+    b, sec, per = cpu_sweep(sizes, dtypes, NBR, threads, steps, args.warmup)
+    wall = time.perf_counter() - t0
+    value = b / sec / 1e9
     line = {
-        "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": args.gpus, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "+".join(dtypes), "data": "synthetic (seeded generator)",
         "impl": "reference",
-        "config": {"workload": WORKLOAD, "block_sizes": sizes, "sample_rows": rows},
+        "config": {"workload": WORKLOAD, "block_sizes": sizes, "n_block_rows": NBR,
+                   "llc": "flushed before every product (256 MB write), outside the timing", "wall_s": round(wall, 1)},
         "cpu_baseline": {"value": round(value, 2), "unit": "GB/s", "cores": threads, "kind": "port",
-                         "sample": f"first {rows} block rows (bs 32: {rows // 2}) of every sweep matrix as CSR; "
-                                   "the reference CPU loop main.cpp:36-45 restated in C, rows split over "
-                                   f"{threads} threads (the reference's main.cpp needs the absent fmt and "
-                                   "cuda_jit submodules, so it is not built)"},
+                         "sample": f"the full {NBR}-block-row sweep matrices as CSR, {steps} products each after "
+                                   f"{args.warmup} untimed; the reference CPU loop main.cpp:36-45 restated in C "
+                                   f"(oracle/oracle.c), rows split over {threads} threads; the reference's main.cpp "
+                                   "needs the absent fmt and cuda_jit submodules, so it is not built",
+                         "per_case_gbs": per},
         "e2e": {"value": round(value, 2), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json_line(line), flush=True)
@@ -688,22 +762,44 @@ def batch_grids(n_systems, seed=0):
     return [(int(nx), max(2, int(round(nx / 4)))) for nx in nxs]
 
 
+def fp64_floor(rp, c, v, bs, x, b):
+    """u ||A| |x|| / ||b||, u = 2^-53: the rounding floor of b - A x evaluated
+    in FP64 for this x (the residual of the correctly rounded solution is of
+    this size too), so a system whose floor exceeds the tolerance cannot be
+    expected to meet it in FP64."""
+    import scipy.sparse as sp
+    n = (len(rp) - 1) * bs
+    A = sp.bsr_matrix((np.abs(np.asarray(v, np.float64)).reshape(-1, bs, bs), c, rp), shape=(n, n))
+    return float(2.0 ** -53 * np.linalg.norm(A @ np.abs(x)) / np.linalg.norm(b))
+
+
 def measure_batch(precisions, tol, max_iters, repeats, n_systems=256, per_request=True, grid=None, shift=None):
     """The uneven batch (nx log-uniform in [20, 400], ny = nx / 4, seeded): each
     precision solved by one persistent, graph-captured launch, and the plain
-    FP64 per-request solver run system after system on the same GPU."""
+    FP64 per-request solver run system after system on the same GPU (its
+    solver objects built before the timed loop, their construction reported
+    as setup_s). Each system's FP64 rounding floor (fp64_floor) is reported
+    beside its true residual where it missed the tolerance."""
     import torch
 
     import block_matrix_format_performance_gb300 as bm
     grids = batch_grids(n_systems) if grid is None else [grid] * n_systems
-    mats, rhs = [], []
+    mats, rhs, host = [], [], []
     for nx, ny in grids:
         rp, c, v, b = shifted_q4(nx, ny, shift) if shift else bm.gen_q4_elasticity(nx, ny)
         mats.append(bm.Matrix.from_bcsr(rp, c, v, 2))
         rhs.append(b)
+        host.append((rp, c, v))
     d_b = [torch.from_numpy(b).cuda() for b in rhs]
     d_x = [torch.empty_like(b) for b in d_b]
     out = {"systems": len(grids), "dofs_total": int(sum(2 * a * b for a, b in grids)), "tol": tol}
+    floors = {}
+
+    def floor_of(k, x):
+        if k not in floors:
+            floors[k] = fp64_floor(*host[k], 2, x, rhs[k])
+        return floors[k]
+
     for prec in precisions:
         batch = bm.Batch(mats, prec, tol=tol, max_iters=max_iters)
         t0 = time.perf_counter()
@@ -717,6 +813,11 @@ def measure_batch(precisions, tol, max_iters, repeats, n_systems=256, per_reques
             times.append(time.perf_counter() - t0)
         batch.close()
         batch_s = min(times)
+        missed = []
+        for k, i in enumerate(infos):
+            if i["status"] != 0:
+                fl = floor_of(k, d_x[k].cpu().numpy())
+                missed.append({"grid": grids[k], "true_rel": i["true_rel_residual"], "fp64_floor": fl})
         out[prec] = {
             "cluster": cluster, "threads_per_cta": threads, "autotune_s": round(tune_s, 3),
             "batch_s": round(batch_s, 4), "solves_per_s": round(len(grids) / batch_s, 2),
@@ -725,20 +826,185 @@ def measure_batch(precisions, tol, max_iters, repeats, n_systems=256, per_reques
             "iterations": sum(i["iterations"] for i in infos),
             "iterations_fp32": sum(i["iterations_fp32"] for i in infos),
             "fp64_fallbacks": sum(i["used_fp64_fallback"] for i in infos),
-            "not_converged": [{"grid": grids[k], "true_rel": i["true_rel_residual"]} for k, i in enumerate(infos)
-                              if i["status"] != 0][:12]}
+            "replacements": sum(i["replacements"] for i in infos),
+            "not_converged": missed[:16],
+            "not_converged_below_floor": sum(m["fp64_floor"] < tol for m in missed)}
     if per_request:
+        t0 = time.perf_counter()
+        solvers = [bm.Solver(m, "fp64", tol=tol, max_iters=max_iters) for m in mats]
+        torch.cuda.synchronize()
+        setup_s = time.perf_counter() - t0
         seq = []
         t0 = time.perf_counter()
-        for m, b, x in zip(mats, d_b, d_x):
-            s = bm.Solver(m, "fp64", tol=tol, max_iters=max_iters)
-            seq.append(s.solve(b, x))
-            s.close()
+        for sv, b, x in zip(solvers, d_b, d_x):
+            seq.append(sv.solve(b, x))
         dt = time.perf_counter() - t0
+        for sv in solvers:
+            sv.close()
         out["per_request_fp64"] = {"seconds": round(dt, 4), "solves_per_s": round(len(grids) / dt, 2),
-                                   "converged": sum(i["status"] == 0 for i in seq)}
+                                   "setup_s": round(setup_s, 3),
+                                   "converged": sum(i["status"] == 0 for i in seq),
+                                   "iterations": sum(i["iterations"] for i in seq)}
+    if grid is None and shift is None:
+        # every system's floor, from its last FP64 solution in d_x
+        xs = [x.cpu().numpy() for x in d_x]
+        fl = [floor_of(k, xs[k]) for k in range(len(grids))]
+        out["fp64_floor_above_tol"] = sum(f > tol for f in fl)
+        out["fp64_floor_max"] = max(fl)
     for m in mats:
         m.close()
+    return out
+
+
+def fem_small(flush, stream):
+    """BASELINE config 0: the 200x50 Q4 plane-stress operator (20 000 DOFs,
+    BCSR bs 2, FP64). SpMV with x uniform in [-1, 1] (seed 0) on the GPU
+    (warm: 3.5 MB stays in L2, as in the reference's own back-to-back timing;
+    and L2-flushed) and on the host (the reference CPU loop, 1 thread and all
+    threads), then the FP64 BiCGStab solve to 1e-10 on both."""
+    import torch
+
+    import block_matrix_format_performance_gb300 as bm
+    from oracle import oracle as orc
+    nx, ny = 200, 50
+    rp, c, v, rhs = bm.gen_q4_elasticity(nx, ny)
+    n = 2 * nx * ny
+    x = bm.gen_uniform_vector(n, 0, X_STREAM)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    dx, dy = torch.from_numpy(x).cuda(), torch.empty(n, dtype=torch.float64, device="cuda")
+    lanes = A.autotune(dx, dy)
+    nbytes = bm.bcsr_spmv_bytes(np.float64, nx * ny, nx * ny, 2, int(c.size))
+    warm_s = replay_seconds(lambda: A.spmv(dx, dy), 100, stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    cold = []
+    for r in range(23):
+        flush()
+        e0.record(stream)
+        A.spmv(dx, dy)
+        e1.record(stream)
+        e1.synchronize()
+        if r >= 3:
+            cold.append(e0.elapsed_time(e1) * 1e-3)
+    cold_s = sum(cold) / len(cold)
+    crp, cc, cv = orc.bcsr_to_csr(rp, c, v, 2)
+    y_ref = orc.csr_spmv(crp, cc, cv, x)
+    err = float(np.sum((dy.cpu().numpy() - y_ref) ** 2) / np.sum(y_ref ** 2))
+    threads = os.cpu_count() or 1
+    cpu = {}
+    for th in (1, threads):
+        yb = np.zeros_like(x)
+        orc.csr_spmv(crp, cc, cv, x, threads=th, out=yb)
+        t0 = time.perf_counter()
+        for _ in range(50):
+            orc.csr_spmv(crp, cc, cv, x, threads=th, out=yb)
+        sec = (time.perf_counter() - t0) / 50
+        cpu[f"threads_{th}"] = {"us": round(sec * 1e6, 2), "gbs": round(nbytes / sec / 1e9, 2)}
+    sv = bm.Solver(A, "fp64", tol=1e-10, max_iters=100000)
+    d_b = torch.from_numpy(rhs).cuda()
+    d_x = torch.empty_like(d_b)
+    infos = [sv.solve(d_b, d_x) for _ in range(3)]
+    sv.close()
+    best = min(infos, key=lambda i: i["seconds"])
+    xs = d_x.cpu().numpy()
+    gpu_solve = {k: best[k] for k in ("iterations", "seconds", "true_rel_residual", "restarts", "replacements",
+                                      "status")}
+    gpu_solve["fp64_floor"] = fp64_floor(rp, c, v, 2, xs, rhs)
+    gpu_solve["us_per_iteration"] = round(best["seconds"] / max(best["iterations"], 1) * 1e6, 2)
+    A.close()
+    return {"workload": "Q4 plane stress 200x50 nodes (E=1, nu=0.3, left edge clamped, f_y=-1 on the right edge), "
+                        "20000 DOFs, BCSR bs 2, FP64",
+            "nnzb": int(c.size), "spmv_bytes": int(nbytes), "lanes": lanes,
+            "gpu_spmv": {"warm_us": round(warm_s * 1e6, 3), "warm_gbs": round(nbytes / warm_s / 1e9, 1),
+                         "l2_flushed_us": round(cold_s * 1e6, 3), "l2_flushed_gbs": round(nbytes / cold_s / 1e9, 1),
+                         "compare_results_error": err,
+                         "note": "3.5 MB: launch- and latency-bound, not an HBM roofline case"},
+            "cpu_spmv": cpu, "gpu_solve": gpu_solve,
+            "cpu_solve": {"threads_1": cpu_solve((nx, ny), 1), f"threads_{threads}": cpu_solve((nx, ny), threads)}}
+
+
+def iteration_roofline(grid, hbm_gbs, fp64_gflops, iters=300):
+    """Live cost of one FP64 BiCGStab iteration of the whole-GPU engine on
+    the Q4 operator, against its two floors: HBM bytes (2 SpMV + 17 n vector
+    elements of 8 bytes) over the measured copy bandwidth, and FP64 FMAs
+    (8 per block for the two bs-2 products, 12 per row for the epilogue dots
+    and vector updates) over the measured FP64 rate. Times `iters`
+    iterations of one solve (the tolerance set out of reach)."""
+    import torch
+
+    import block_matrix_format_performance_gb300 as bm
+    nx, ny = grid
+    rp, c, v, rhs = bm.gen_q4_elasticity(nx, ny)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    n, nnzb = 2 * nx * ny, int(c.size)
+    sv = bm.Solver(A, "fp64", tol=1e-30, max_iters=iters)
+    d_b = torch.from_numpy(rhs).cuda()
+    d_x = torch.empty_like(d_b)
+    sv.solve(d_b, d_x)
+    info = min((sv.solve(d_b, d_x) for _ in range(2)), key=lambda i: i["seconds"])
+    sv.close()
+    A.close()
+    us = info["seconds"] / max(info["iterations"], 1) * 1e6
+    nbytes = 2 * bm.bcsr_spmv_bytes(np.float64, nx * ny, nx * ny, 2, nnzb) + 17 * n * 8
+    fmas = 8 * nnzb + 12 * n
+    hbm_us = nbytes / (hbm_gbs * 1e9) * 1e6
+    fp64_us = 2 * fmas / (fp64_gflops * 1e9) * 1e6
+    floor = max(hbm_us, fp64_us)
+    return {"grid": [nx, ny], "dofs": n, "iterations_timed": info["iterations"], "us_per_iteration": round(us, 2),
+            "bytes_per_iteration": int(nbytes), "fp64_fmas_per_iteration": int(fmas),
+            "hbm_floor_us": round(hbm_us, 2), "fp64_floor_us": round(fp64_us, 2),
+            "floor_us": round(floor, 2), "of_floor": round(floor / us, 3)}
+
+
+def fem_large(cpu_iters=(12, 60)):
+    """BASELINE config 2: the Q4 operator on 2000x500 nodes (2 M DOFs, BCSR
+    bs 2). Plain FP64 BiCGStab and FP32-inner / FP64-refined, both to 1e-10
+    relative residual: iterations, time, true residual, the FP64 floor, and
+    the mixed solution's error against the FP64 one. The CPU baseline runs
+    the same recurrences for a bounded number of iterations (1 thread and all
+    threads) and projects the GPU's iteration count at that rate."""
+    import torch
+
+    import block_matrix_format_performance_gb300 as bm
+    from oracle import oracle as orc
+    nx, ny = 2000, 500
+    rp, c, v, rhs = bm.gen_q4_elasticity(nx, ny)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    d_b = torch.from_numpy(rhs).cuda()
+    out, xs = {}, {}
+    for prec in ("fp64", "mixed"):
+        t0 = time.perf_counter()
+        sv = bm.Solver(A, prec, tol=1e-10, max_iters=200000)
+        setup = time.perf_counter() - t0
+        d_x = torch.empty_like(d_b)
+        info = sv.solve(d_b, d_x)
+        sv.close()
+        xs[prec] = d_x.cpu().numpy()
+        out[prec] = {k: info[k] for k in ("iterations", "iterations_fp32", "seconds", "true_rel_residual", "restarts",
+                                          "replacements", "used_fp64_fallback", "status")}
+        out[prec]["setup_s"] = round(setup, 3)
+        out[prec]["fp64_floor"] = fp64_floor(rp, c, v, 2, xs[prec], rhs)
+        out[prec]["us_per_iteration"] = round(info["seconds"] / max(info["iterations"], 1) * 1e6, 2)
+    out["mixed_error_vs_fp64"] = float(np.linalg.norm(xs["mixed"] - xs["fp64"]) / np.linalg.norm(xs["fp64"]))
+    out["mixed_speedup"] = round(out["fp64"]["seconds"] / out["mixed"]["seconds"], 3)
+    A.close()
+    crp, cc, cv = orc.bcsr_to_csr(rp, c, v, 2)
+    del rp, c, v
+    threads = os.cpu_count() or 1
+    cpu = {}
+    for th, k in zip((1, threads), cpu_iters):
+        t0 = time.perf_counter()
+        if th == 1:
+            _, st, it, rel = orc.bicgstab(crp, cc, cv, rhs, 1e-30, k)
+        else:
+            _, st, it, rel = orc.bicgstab_mt(crp, cc, cv, rhs, 1e-30, k, th)
+        sec = time.perf_counter() - t0
+        per_it = sec / max(it, 1)
+        cpu[f"threads_{th}"] = {"iterations_timed": it, "s_per_iteration": round(per_it, 5),
+                                "projected_solve_s": round(per_it * out["fp64"]["iterations"], 1)}
+    out["cpu_solve"] = cpu
+    out["cpu_solve"]["note"] = ("the reference recurrences (oracle.c) run for a bounded number of iterations; "
+                                "projected_solve_s = s_per_iteration x the GPU FP64 solve's iterations")
+    out["workload"] = "Q4 plane stress 2000x500 nodes, 2000000 DOFs, BCSR bs 2, nnzb 8985004"
     return out
 
 
@@ -764,20 +1030,15 @@ def serve_stream(n_requests, rate, seed=1, large_fraction=0.05):
     return arrivals, grids
 
 
-def run_serve(args):
-    """Served solve stream through the continuous-batching server, and the
-    same stream's head on the plain FP64 per-request solver (FIFO)."""
-    import threading
-
-    import torch
-
+def serve_inputs(n_requests, rate, large_fraction, matrix="q4", shift=1e-3, seed=1):
+    """The request stream (serve_stream), its distinct matrices as device
+    handles and every request's right-hand side (uniform in [-1, 1), 0 on
+    the clamped column)."""
     import block_matrix_format_performance_gb300 as bm
-    from block_matrix_format_performance_gb300 import build as B
-    B.build()
-    arrivals, grids = serve_stream(args.requests, args.rate, large_fraction=args.large_fraction)
+    arrivals, grids = serve_stream(n_requests, rate, seed=seed, large_fraction=large_fraction)
     mats = {}
     for g in sorted(set(grids)):
-        rp, c, v, _ = shifted_q4(*g, args.shift) if args.matrix == "shifted" else bm.gen_q4_elasticity(*g)
+        rp, c, v, _ = shifted_q4(*g, shift) if matrix == "shifted" else bm.gen_q4_elasticity(*g)
         mats[g] = bm.Matrix.from_bcsr(rp, c, v, 2)
     rng = np.random.default_rng(7)
     rhs = []
@@ -785,22 +1046,21 @@ def run_serve(args):
         b = rng.uniform(-1, 1, 2 * nx * ny)
         b.reshape(ny, nx, 2)[:, 0, :] = 0.0  # clamped column carries no load
         rhs.append(b)
+    return arrivals, grids, mats, rhs
+
+
+def serve_once(precision, arrivals, grids, mats, rhs, tol, max_iters, **kw):
+    """One pass of the stream through the continuous-batching server:
+    requests submitted at their arrival times from a producer thread,
+    latency = submit to completion (bmfp_solve_info.seconds)."""
+    import threading
+
+    import block_matrix_format_performance_gb300 as bm
     xs = [np.zeros_like(b) for b in rhs]
-    kw = {}
-    if args.wide_lanes is not None:
-        kw["wide_lanes"] = args.wide_lanes
-    if args.wide_threshold is not None:
-        kw["wide_threshold_rows"] = args.wide_threshold
-    if args.cluster_size is not None:
-        kw["cluster_size"] = args.cluster_size
-    if args.threads_per_cta is not None:
-        kw["threads_per_cta"] = args.threads_per_cta
-    if args.ctas_per_sm:
-        kw["ctas_per_sm"] = args.ctas_per_sm
-    srv = bm.Server(args.precision, tol=args.tol, max_iters=args.max_iters, **kw)
-    # warm-up: one small request
-    w = np.zeros(mats[min(mats)].rows)
-    srv.wait(srv.submit(mats[min(mats)], np.ones_like(w), w))
+    srv = bm.Server(precision, tol=tol, max_iters=max_iters, **kw)
+    small = min(mats)
+    w = np.zeros(mats[small].rows)
+    srv.wait(srv.submit(mats[small], np.ones_like(w), w))  # warm-up
     tickets = [None] * len(grids)
     t_start = time.perf_counter()
 
@@ -814,56 +1074,142 @@ def run_serve(args):
     th = threading.Thread(target=producer)
     th.start()
     th.join()
-    infos = []
-    for t in tickets:
-        infos.append(srv.wait(t))
+    infos = [srv.wait(t) for t in tickets]
     makespan = time.perf_counter() - t_start
     stats = srv.stats()
-    srv_opts = {"wide_lanes": srv.options.wide_lanes, "wide_threshold_rows": srv.options.wide_threshold_rows}
+    opts = {"wide_lanes": srv.options.wide_lanes, "wide_threshold_rows": srv.options.wide_threshold_rows}
     srv.close()
     lat = np.array([i["seconds"] for i in infos])
-    conv = sum(i["status"] == 0 for i in infos)
-    # Baseline: the plain FP64 per-request solver serving the same stream FIFO
-    # on one GPU. Each distinct grid's solve is timed once on the device and
-    # the queue is replayed with those service times.
-    solvers, service_by_grid = {}, {}
+    bad = [{"grid": list(grids[k]), "status": i["status"], "true_rel": i["true_rel_residual"]}
+           for k, i in enumerate(infos) if i["status"] != 0]
+    return {"precision": precision, "requests": len(grids), "makespan_s": round(makespan, 3),
+            "solves_per_s": round(len(grids) / makespan, 2),
+            "latency_p50_s": round(float(np.percentile(lat, 50)), 4),
+            "latency_p99_s": round(float(np.percentile(lat, 99)), 4),
+            "converged": sum(i["status"] == 0 for i in infos),
+            "worst_true_rel": max(i["true_rel_residual"] for i in infos),
+            "iterations": sum(i["iterations"] for i in infos),
+            "iterations_fp32": sum(i["iterations_fp32"] for i in infos),
+            "micro_batches": stats["micro_batches"], "wide_solves": stats["wide_solves"],
+            "peak_device_bytes": stats["peak_bytes"], **opts, "not_converged": bad[:12]}, xs
+
+
+def fifo_baseline(arrivals, grids, mats, rhs, tol, max_iters):
+    """The plain FP64 per-request solver (the reference's path: one
+    gpu_bicgstab solve per request, gpu/bicgstab.cu:387-526, here the
+    whole-GPU engine) serving the stream first in, first out in real time:
+    each request waits for its arrival and for the request before it, then
+    its own right-hand side goes to the device, is solved, and x comes back.
+    One solver per distinct matrix is built before the stream starts
+    (setup_s). Returns the summary and every request's service time."""
+    import torch
+
+    import block_matrix_format_performance_gb300 as bm
+    t0 = time.perf_counter()
+    solvers = {g: bm.Solver(m, "fp64", tol=tol, max_iters=max_iters) for g, m in mats.items()}
+    torch.cuda.synchronize()
+    setup = time.perf_counter() - t0
+    service, lat, infos = [], [], []
+    t_start = time.perf_counter()
     for k, g in enumerate(grids):
-        if args.no_baseline:
-            break
-        if g in service_by_grid:
-            continue
-        s = bm.Solver(mats[g], "fp64", tol=args.tol, max_iters=args.max_iters)
+        now = time.perf_counter() - t_start
+        if arrivals[k] > now:
+            time.sleep(arrivals[k] - now)
+        s0 = time.perf_counter()
         d_b = torch.from_numpy(rhs[k]).cuda()
         d_x = torch.empty_like(d_b)
-        t0 = time.perf_counter()
-        s.solve(d_b, d_x)
-        service_by_grid[g] = time.perf_counter() - t0
-        s.close()
-    done, base_lat = 0.0, []
-    for k, g in enumerate(grids):
-        if args.no_baseline:
-            break
-        done = max(done, arrivals[k]) + service_by_grid[g]
-        base_lat.append(done - arrivals[k])
-    base_tput = len(grids) / max(done, 1e-9)
-    nb = len(grids)
-    baseline = None if args.no_baseline else {
-        "requests": nb, "distinct_grids_timed": len(service_by_grid), "solves_per_s": round(base_tput, 2),
-        "latency_p50_s": round(float(np.percentile(base_lat, 50)), 4),
-        "latency_p99_s": round(float(np.percentile(base_lat, 99)), 4)}
-    bad = [{"grid": list(grids[k]), "status": i["status"], "true_rel": i["true_rel_residual"]}
-           for k, i in enumerate(infos) if i["status"] != 0][:12]
-    print(json_line({
-        "workload": "serve", "matrix": "q4" if args.matrix == "q4" else f"q4+{args.shift:g}I",
-        "requests": len(grids), "rate_req_s": args.rate, "precision": args.precision,
-        "tol": args.tol, "large_requests": int(sum(g == (1000, 250) for g in grids)),
-        "makespan_s": round(makespan, 3), "solves_per_s": round(len(grids) / makespan, 2),
-        "latency_p50_s": round(float(np.percentile(lat, 50)), 4), "latency_p99_s": round(float(np.percentile(lat, 99)), 4),
-        "converged": conv, "worst_true_rel": max(i["true_rel_residual"] for i in infos),
-        "micro_batches": stats["micro_batches"], "wide_solves": stats["wide_solves"],
-        "peak_device_bytes": stats["peak_bytes"], "wide_lanes": srv_opts["wide_lanes"],
-        "wide_threshold_rows": srv_opts["wide_threshold_rows"], "not_converged": bad,
-        "per_request_fp64": baseline}), flush=True)
+        infos.append(solvers[g].solve(d_b, d_x))
+        d_x.cpu()
+        s1 = time.perf_counter()
+        service.append(s1 - s0)
+        lat.append(s1 - t_start - arrivals[k])
+    makespan = time.perf_counter() - t_start
+    for sv in solvers.values():
+        sv.close()
+    return {"setup_s": round(setup, 3), "makespan_s": round(makespan, 3),
+            "solves_per_s": round(len(grids) / makespan, 2),
+            "latency_p50_s": round(float(np.percentile(lat, 50)), 4),
+            "latency_p99_s": round(float(np.percentile(lat, 99)), 4),
+            "converged": sum(i["status"] == 0 for i in infos)}, service
+
+
+def fifo_timeline(arrivals, service):
+    """FIFO completion times of one server with the given service times:
+    done_k = max(done_{k-1}, arrival_k) + service_k."""
+    done, lat = 0.0, []
+    for a, sv in zip(arrivals, service):
+        done = max(done, a) + sv
+        lat.append(done - a)
+    return {"makespan_s": round(done, 3), "solves_per_s": round(len(arrivals) / done, 2),
+            "latency_p50_s": round(float(np.percentile(lat, 50)), 4),
+            "latency_p99_s": round(float(np.percentile(lat, 99)), 4)}
+
+
+def serve_suite(n_requests, rate, precisions, sustained_factor, tol=1e-10, max_iters=100000, large_fraction=0.05,
+                sustained_requests=None):
+    """BASELINE config 4 in the bench line: the stream at the stated rate
+    through the server in each precision; the same requests at a rate the
+    server sustains (sustained_factor x the first server's throughput at
+    the stated rate, so that arrivals do not outrun it; the same exponential
+    draws rescaled); and the plain FP64 per-request solver serving the
+    stated-rate stream FIFO, every request solved in real time (the
+    sustained stream's FIFO latencies follow from the same requests'
+    measured service times)."""
+    arrivals, grids, mats, rhs = serve_inputs(n_requests, rate, large_fraction)
+    out = {"workload": f"Poisson arrivals, {n_requests} requests, grids as the uneven batch plus "
+                       f"{large_fraction:.0%} 1000x250, random loads, tol {tol:g}, 120 GB HBM budget",
+           "large_requests": int(sum(g == (1000, 250) for g in grids))}
+    for prec in precisions:
+        res, _ = serve_once(prec, arrivals, grids, mats, rhs, tol, max_iters)
+        res["rate_req_s"] = rate
+        out[f"served_{prec}_at_{rate:g}"] = res
+    first = out[f"served_{precisions[0]}_at_{rate:g}"]
+    sus_rate = round(sustained_factor * first["solves_per_s"], 1)
+    ns = sustained_requests or n_requests
+    sus_arr = arrivals[:ns] * (rate / sus_rate)
+    res, _ = serve_once(precisions[0], sus_arr, grids[:ns], mats, rhs[:ns], tol, max_iters)
+    res["rate_req_s"] = sus_rate
+    out[f"served_{precisions[0]}_sustained"] = res
+    base, service = fifo_baseline(arrivals, grids, mats, rhs, tol, max_iters)
+    base["rate_req_s"] = rate
+    out[f"fifo_plain_fp64_at_{rate:g}"] = base
+    sus = fifo_timeline(sus_arr, service[:ns])
+    sus["rate_req_s"] = sus_rate
+    sus["note"] = "FIFO timeline of the same requests' measured service times"
+    out["fifo_plain_fp64_sustained"] = sus
+    for m in mats.values():
+        m.close()
+    return out
+
+
+def run_serve(args):
+    """Served solve stream through the continuous-batching server, and the
+    same stream on the plain FP64 per-request solver (FIFO, every request
+    solved)."""
+    from block_matrix_format_performance_gb300 import build as B
+    B.build()
+    arrivals, grids, mats, rhs = serve_inputs(args.requests, args.rate, args.large_fraction, args.matrix, args.shift)
+    kw = {}
+    if args.wide_lanes is not None:
+        kw["wide_lanes"] = args.wide_lanes
+    if args.wide_threshold is not None:
+        kw["wide_threshold_rows"] = args.wide_threshold
+    if args.cluster_size is not None:
+        kw["cluster_size"] = args.cluster_size
+    if args.threads_per_cta is not None:
+        kw["threads_per_cta"] = args.threads_per_cta
+    if args.ctas_per_sm:
+        kw["ctas_per_sm"] = args.ctas_per_sm
+    res, _ = serve_once(args.precision, arrivals, grids, mats, rhs, args.tol, args.max_iters, **kw)
+    base = None
+    if not args.no_baseline:
+        base, _ = fifo_baseline(arrivals, grids, mats, rhs, args.tol, args.max_iters)
+    for m in mats.values():
+        m.close()
+    print(json_line({"workload": "serve", "matrix": "q4" if args.matrix == "q4" else f"q4+{args.shift:g}I",
+                     "rate_req_s": args.rate, "tol": args.tol,
+                     "large_requests": int(sum(g == (1000, 250) for g in grids)),
+                     **res, "per_request_fp64": base}), flush=True)
 
 
 def measure_variants(rp, c, v, bs, x, runs, stream):

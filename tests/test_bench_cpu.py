@@ -40,3 +40,16 @@ def test_json_lines_are_strict():
     import bench
     line = bench.json_line({"e2e": {"value": float("nan"), "s": float("inf")}, "v": [1.5, float("-inf")], "k": 2})
     assert json.loads(line, parse_constant=_no_nan) == {"e2e": {"value": None, "s": None}, "v": [1.5, None], "k": 2}
+
+
+def test_reference_arm_loads_no_product_code(orc):
+    """The reference arm times the oracle's restatement of the reference CPU
+    loop on matrices from the oracle's own generator: the product package
+    (and its libbmfp.so) is never imported."""
+    code = ("import sys, types; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0', "
+            "'--sizes', '2', '--dtypes', 'f32']; import bench; bench.main(); "
+            "assert not any(m.startswith('block_matrix_format_performance_gb300') for m in sys.modules), "
+            "sorted(m for m in sys.modules if 'block_matrix' in m)")
+    p = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert p.returncode == 0, p.stderr[-2000:]
+    assert json.loads(p.stdout.strip().splitlines()[-1])["impl"] == "reference"
