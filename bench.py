@@ -78,7 +78,8 @@ def parse_args():
     ap.add_argument("--serve-requests", type=int, default=5000, help="line: requests of the served stream")
     ap.add_argument("--sustained-requests", type=int, default=None,
                     help="line: requests of the sustained-rate stream (default: --serve-requests)")
-    ap.add_argument("--serve-precisions", default="fp64,mixed", help="line: server precisions at the stated rate")
+    ap.add_argument("--serve-precisions", default="mixed",
+                    help="line: server precisions at the stated rate (the first also runs at the sustained rate)")
     ap.add_argument("--sustained-factor", type=float, default=0.7,
                     help="line: sustained rate as a fraction of the first server's throughput at the stated rate")
     ap.add_argument("--no-autotune", action="store_true",
@@ -88,7 +89,7 @@ def parse_args():
     ap.add_argument("--dtypes", default=",".join(DTYPES))
     ap.add_argument("--n-block-rows", type=int, default=NBR,
                     help="block rows per matrix (smaller only for profiling captures)")
-    ap.add_argument("--workload", choices=("spmv", "solve", "batch", "serve", "ndiag", "bridge"), default="spmv",
+    ap.add_argument("--workload", choices=("spmv", "solve", "batch", "serve", "ndiag", "bridge", "precond"), default="spmv",
                     help="spmv: the block-size sweep line (default); solve: one Q4 elasticity solve; "
                          "batch: 256 uneven Q4 systems in one persistent launch; serve: Poisson request "
                          "stream through the server; ndiag: every variant on gen_n_diag_bcsr matrices, "
@@ -115,6 +116,8 @@ def parse_args():
                     help="solve: Q4 elasticity K (default) or the implicit-step operator K + shift * I")
     ap.add_argument("--shift", type=float, default=1e-3, help="solve: shift of --matrix shifted")
     ap.add_argument("--precision", default="fp64", choices=("fp64", "fp32", "mixed", "both"))
+    ap.add_argument("--preconditioner", default="none", choices=("none", "jacobi", "block_jacobi"),
+                    help="solve: right preconditioner of the single-system solver")
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--max-iters", type=int, default=200000)
     ap.add_argument("--repeats", type=int, default=3)
@@ -518,14 +521,16 @@ def run_ours(args):
     # The FEM workloads of configs 0 and 2, the live cost of one solver
     # iteration against its floors, and the served stream of config 4.
     fem = None
-    if not args.no_fem:
+    single = rank == 0 and world == 1  # the FEM and serving legs are one-GPU workloads
+    if single and not args.no_fem:
         t0 = time.perf_counter()
         fem = {"config0_200x50": fem_small(flush, stream),
                "iteration_roofline": [iteration_roofline(g, hbm, fp64_gflops) for g in ((1000, 250), (2000, 500))],
-               "config2_2000x500": fem_large()}
+               "config2_2000x500": fem_large(),
+               "preconditioners": precond_compare(((1000, 250), (2000, 500)))}
         fem["wall_s"] = round(time.perf_counter() - t0, 1)
     serve = None
-    if not args.no_serve:
+    if single and not args.no_serve:
         t0 = time.perf_counter()
         serve = serve_suite(args.serve_requests, args.rate, args.serve_precisions.split(","), args.sustained_factor,
                             sustained_requests=args.sustained_requests)
@@ -717,7 +722,7 @@ def run_solve(args):
     out, xs = {}, {}
     for prec in (("fp64", "mixed") if args.precision == "both" else (args.precision,)):
         kw = {"ctas_per_sm": args.ctas_per_sm} if args.ctas_per_sm else {}
-        s = bm.Solver(A, prec, tol=args.tol, max_iters=args.max_iters, **kw)
+        s = bm.Solver(A, prec, tol=args.tol, max_iters=args.max_iters, preconditioner=args.preconditioner, **kw)
         d_x = torch.empty_like(d_b)
         infos = [s.solve(d_b, d_x) for _ in range(max(1, args.repeats))]
         s.close()
@@ -953,6 +958,30 @@ def iteration_roofline(grid, hbm_gbs, fp64_gflops, iters=300):
             "bytes_per_iteration": int(nbytes), "fp64_fmas_per_iteration": int(fmas),
             "hbm_floor_us": round(hbm_us, 2), "fp64_floor_us": round(fp64_us, 2),
             "floor_us": round(floor, 2), "of_floor": round(floor / us, 3)}
+
+
+def precond_compare(grids, tol=1e-10, max_iters=200000):
+    """FP64 BiCGStab on the Q4 operator with no preconditioner, point
+    Jacobi (gpu/bicgstab.cu:201-238) and block Jacobi (the 2x2 diagonal
+    blocks inverted): iterations, seconds and the true residual of each."""
+    import torch
+
+    import block_matrix_format_performance_gb300 as bm
+    out = {}
+    for nx, ny in grids:
+        rp, c, v, rhs = bm.gen_q4_elasticity(nx, ny)
+        A = bm.Matrix.from_bcsr(rp, c, v, 2)
+        d_b = torch.from_numpy(rhs).cuda()
+        res = {}
+        for pre in ("none", "jacobi", "block_jacobi"):
+            sv = bm.Solver(A, "fp64", tol=tol, max_iters=max_iters, preconditioner=pre)
+            d_x = torch.empty_like(d_b)
+            info = sv.solve(d_b, d_x)
+            sv.close()
+            res[pre] = {k: info[k] for k in ("iterations", "seconds", "true_rel_residual", "restarts", "status")}
+        out[f"{nx}x{ny}"] = res
+        A.close()
+    return out
 
 
 def fem_large(cpu_iters=(12, 60)):
@@ -1388,6 +1417,12 @@ def main():
         return
     if args.workload == "batch":
         run_batch(args)
+        return
+    if args.workload == "precond":
+        from block_matrix_format_performance_gb300 import build as B
+        B.build()
+        grid = tuple(int(t) for t in args.grid.lower().split("x"))
+        print(json_line({"workload": "precond", **precond_compare([grid], args.tol, args.max_iters)}), flush=True)
         return
     if args.workload == "ndiag":
         run_ndiag(args)

@@ -367,7 +367,7 @@ class Matrix:
 
 
 SOLVE_FP64, SOLVE_FP32, SOLVE_MIXED = 0, 1, 2
-PRECOND_NONE, PRECOND_JACOBI = 0, 1
+PRECOND_NONE, PRECOND_JACOBI, PRECOND_BLOCK_JACOBI = 0, 1, 2
 _PRECISIONS = {"fp64": SOLVE_FP64, "fp32": SOLVE_FP32, "mixed": SOLVE_MIXED}
 
 
@@ -382,7 +382,7 @@ def solver_options(base=None, **kw) -> SolverOptions:
         if k == "precision" and isinstance(v, str):
             v = _PRECISIONS[v]
         if k == "preconditioner" and isinstance(v, str):
-            v = {"none": PRECOND_NONE, "jacobi": PRECOND_JACOBI}[v]
+            v = {"none": PRECOND_NONE, "jacobi": PRECOND_JACOBI, "block_jacobi": PRECOND_BLOCK_JACOBI}[v]
         setattr(o, k, int(v) if isinstance(v, bool) else v)
     return o
 

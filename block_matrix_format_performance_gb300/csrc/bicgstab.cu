@@ -371,11 +371,50 @@ __global__ void __launch_bounds__ (kThreads)
     }
 }
 
+// Preconditioner of the vector phases (right preconditioning, q = M^-1 p,
+// z = M^-1 s): none, point Jacobi (gpu/bicgstab.cu:201-238), or block
+// Jacobi (M^-1 = the inverses of the bs x bs diagonal blocks), the latter
+// for bs = 2 with the block in registers and for any bs <= 8 (a block and
+// its inverse fit a thread's registers and a small local frame; the FEM
+// operators this serves have bs 2 or 3).
+enum PreKind
+{
+  kPreNone = 0,
+  kPrePoint = 1,
+  kPreBlock2 = 2,
+  kPreBlockAny = 3
+};
+
+constexpr int kMaxBlockJacobi = 8;
+
+// One block row of a phase with block Jacobi: out = new values of the block
+// (computed by f(k) for k < bs, stored to dst), then prec = Minv * out.
+template <typename T, int PK, class F>
+__device__ __forceinline__ void block_row_apply (const Args<T> &a, int64_t br, T *dst, T *prec, F f)
+{
+  const int bs = PK == kPreBlock2 ? 2 : a.bs;
+  const int64_t base = br * bs;
+  const T *M = a.P + (size_t) br * bs * bs;
+  T u[PK == kPreBlock2 ? 2 : kMaxBlockJacobi];
+  for (int k = 0; k < bs; k++)
+    {
+      u[k] = f (base + k);
+      dst[base + k] = u[k];
+    }
+  for (int r = 0; r < bs; r++)
+    {
+      T acc = 0;
+      for (int c = 0; c < bs; c++)
+        acc = fma (M[r * bs + c], u[c], acc);
+      prec[base + r] = acc;
+    }
+}
+
 // phase 1
 // GB300's FP64 pipe is narrow (about 1/58 of FP32), so the scalar divides and
 // square roots run once per CTA (thread 0) and reach the other threads
 // through shared memory instead of being evaluated by every thread.
-template <typename T, bool PRE>
+template <typename T, int PK>
 __global__ void __launch_bounds__ (kThreads) phase_p (Args<T> a)
 {
   DevState *st = a.st;
@@ -475,6 +514,15 @@ __global__ void __launch_bounds__ (kThreads) phase_p (Args<T> a)
       return;
     }
   const T tb = (T) sh_beta, tw = (T) sh_omega;
+  if constexpr (PK >= kPreBlock2)
+    {
+      // block Jacobi: one block row per thread, q = Minv p of the block
+      for (int64_t br = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; br < a.nbr; br += stride)
+        block_row_apply<T, PK> (a, br, a.p, a.q,
+                                [&] (int64_t i) { return a.r[i] + tb * (a.p[i] - tw * a.v[i]); });
+      return;
+    }
+  const bool PRE = PK == kPrePoint;
   // Four grid-stride elements per pass, loads first (the arrays may alias as
   // far as the compiler knows, so it would not hoist them itself).
   int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
@@ -507,7 +555,7 @@ __global__ void __launch_bounds__ (kThreads) phase_p (Args<T> a)
 }
 
 // phase 3
-template <typename T, bool PRE>
+template <typename T, int PK>
 __global__ void __launch_bounds__ (kThreads) phase_s (Args<T> a)
 {
   DevState *st = a.st;
@@ -544,6 +592,13 @@ __global__ void __launch_bounds__ (kThreads) phase_s (Args<T> a)
     return;
   const T ta = (T) alpha;
   const int64_t stride = (int64_t) gridDim.x * blockDim.x;
+  if constexpr (PK >= kPreBlock2)
+    {
+      for (int64_t br = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; br < a.nbr; br += stride)
+        block_row_apply<T, PK> (a, br, a.s, a.z, [&] (int64_t i) { return a.r[i] - ta * a.v[i]; });
+      return;
+    }
+  const bool PRE = PK == kPrePoint;
   int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
   for (; i + 3 * stride < a.n; i += 4 * stride)
     {
@@ -573,7 +628,7 @@ __global__ void __launch_bounds__ (kThreads) phase_s (Args<T> a)
 }
 
 // phase 5
-template <typename T, bool PRE>
+template <typename T, int PK>
 __global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
 {
   DevState *st = a.st;
@@ -614,8 +669,8 @@ __global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
   // (x', x') feeds the replacement bound only: skipped (0) when it is off.
   const bool track = st->eps > 0.0;
   T rhr = 0, rr = 0, xx = 0;
-  const T *qa = PRE ? a.q : a.p;
-  const T *za = PRE ? a.z : a.s;
+  const T *qa = PK != kPreNone ? a.q : a.p;
+  const T *za = PK != kPreNone ? a.z : a.s;
   const int64_t stride = (int64_t) gridDim.x * blockDim.x;
   int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
   for (; i + 3 * stride < a.n; i += 4 * stride)
@@ -736,6 +791,78 @@ __global__ void jacobi_kernel (int nbr, int bs, const int *rp, const int *cols, 
   }
 }
 
+// Block Jacobi: Minv[br] = inverse of the diagonal block of block row br
+// (Gauss-Jordan with partial pivoting in FP64, one thread per block row),
+// the identity when the row stores no diagonal block or a pivot falls below
+// 1e-20 times the block's largest entry: the block form of the point rule
+// above (1 where |a_ii| < 1e-20 or no diagonal is stored).
+template <typename T>
+__global__ void block_jacobi_kernel (int nbr, int bs, const int *rp, const int *cols, const T *vals, T *Minv)
+{
+  GRID_STRIDE (br, (int64_t) nbr)
+  {
+    const int e = bs * bs;
+    T *out = Minv + (size_t) br * e;
+    const T *blk = nullptr;
+    for (int b = rp[br]; b < rp[br + 1]; b++)
+      if (cols[b] == (int) br)
+        {
+          blk = vals + (size_t) b * e;
+          break;
+        }
+    double a[kMaxBlockJacobi * kMaxBlockJacobi], inv[kMaxBlockJacobi * kMaxBlockJacobi];
+    double amax = 0.0;
+    for (int k = 0; k < e; k++)
+      {
+        a[k] = blk ? (double) blk[k] : 0.0;
+        inv[k] = (k / bs == k % bs) ? 1.0 : 0.0;
+        amax = fmax (amax, fabs (a[k]));
+      }
+    bool ok = blk != nullptr && amax > 0.0;
+    for (int c = 0; c < bs && ok; c++)
+      {
+        int piv = c;
+        for (int r = c + 1; r < bs; r++)
+          if (fabs (a[r * bs + c]) > fabs (a[piv * bs + c]))
+            piv = r;
+        if (!(fabs (a[piv * bs + c]) >= 1e-20 * amax))
+          {
+            ok = false;
+            break;
+          }
+        if (piv != c)
+          for (int k = 0; k < bs; k++)
+            {
+              double t = a[c * bs + k];
+              a[c * bs + k] = a[piv * bs + k];
+              a[piv * bs + k] = t;
+              t = inv[c * bs + k];
+              inv[c * bs + k] = inv[piv * bs + k];
+              inv[piv * bs + k] = t;
+            }
+        const double d = 1.0 / a[c * bs + c];
+        for (int k = 0; k < bs; k++)
+          {
+            a[c * bs + k] *= d;
+            inv[c * bs + k] *= d;
+          }
+        for (int r = 0; r < bs; r++)
+          if (r != c)
+            {
+              const double f = a[r * bs + c];
+              if (f != 0.0)
+                for (int k = 0; k < bs; k++)
+                  {
+                    a[r * bs + k] -= f * a[c * bs + k];
+                    inv[r * bs + k] -= f * inv[c * bs + k];
+                  }
+            }
+      }
+    for (int k = 0; k < e; k++)
+      out[k] = ok ? (T) inv[k] : (T) ((k / bs == k % bs) ? 1 : 0);
+  }
+}
+
 // ------------------------------------------------------------ dispatch
 
 enum SpmvKind
@@ -849,15 +976,26 @@ Args<T> make_args (const bmfp_matrix_s *A, int64_t n, void *x, void *r, void *rh
   return a;
 }
 
-template <typename T, bool PRE>
-void launch_vector_phase (int phase, const Args<T> &a, cudaStream_t s)
+template <typename T, int PK>
+void launch_vector_phase_k (int phase, const Args<T> &a, cudaStream_t s)
 {
   if (phase == 1)
-    phase_p<T, PRE><<<a.grid, kThreads, 0, s>>> (a);
+    phase_p<T, PK><<<a.grid, kThreads, 0, s>>> (a);
   else if (phase == 3)
-    phase_s<T, PRE><<<a.grid, kThreads, 0, s>>> (a);
+    phase_s<T, PK><<<a.grid, kThreads, 0, s>>> (a);
   else
-    phase_x<T, PRE><<<a.grid, kThreads, 0, s>>> (a);
+    phase_x<T, PK><<<a.grid, kThreads, 0, s>>> (a);
+}
+
+template <typename T> void launch_vector_phase (int pk, int phase, const Args<T> &a, cudaStream_t s)
+{
+  switch (pk)
+    {
+    case kPrePoint: launch_vector_phase_k<T, kPrePoint> (phase, a, s); break;
+    case kPreBlock2: launch_vector_phase_k<T, kPreBlock2> (phase, a, s); break;
+    case kPreBlockAny: launch_vector_phase_k<T, kPreBlockAny> (phase, a, s); break;
+    default: launch_vector_phase_k<T, kPreNone> (phase, a, s); break;
+    }
 }
 
 // Unit roundoff of the engine's precision (replacement bound).
@@ -916,18 +1054,22 @@ WideEngine::~WideEngine ()
     cudaFreeHost (h_state_);
 }
 
-int WideEngine::init (const bmfp_matrix_s *A, bool jacobi, int chunk, cudaStream_t stream, int ctas_per_sm)
+int WideEngine::init (const bmfp_matrix_s *A, int precond, int chunk, cudaStream_t stream, int ctas_per_sm)
 {
   if (!A)
     return fail (BMFP_ERROR_INVALID_VALUE, "null matrix");
   const int bs = A->bs ? A->bs : 1;
+  if (precond == BMFP_PRECOND_BLOCK_JACOBI && bs > kMaxBlockJacobi)
+    return fail (BMFP_ERROR_NOT_SUPPORTED, "block Jacobi takes bs <= %d (bs %d)", kMaxBlockJacobi, bs);
   if (A->bs && A->n_rows != A->n_cols)
     return fail (BMFP_ERROR_INVALID_VALUE, "BiCGStab needs a square matrix");
   if (!A->bs && A->n_rows != A->n_cols)
     return fail (BMFP_ERROR_INVALID_VALUE, "BiCGStab needs a square matrix");
   A_ = A;
   dtype_ = A->dtype;
-  jacobi_ = jacobi;
+  jacobi_ = precond != BMFP_PRECOND_NONE;
+  const bool block = precond == BMFP_PRECOND_BLOCK_JACOBI;
+  pre_kind_ = !jacobi_ ? kPreNone : !block ? kPrePoint : bs == 2 ? kPreBlock2 : kPreBlockAny;
   replace_ = dtype_ == BMFP_R64F;
   chunk_ = std::max (1, std::min (chunk, 256));
   n_ = (int64_t) A->n_rows * bs;
@@ -948,8 +1090,14 @@ int WideEngine::init (const bmfp_matrix_s *A, bool jacobi, int chunk, cudaStream
     {
       BMFP_CUDA (cudaMalloc (&q_, vb));
       BMFP_CUDA (cudaMalloc (&z_, vb));
-      BMFP_CUDA (cudaMalloc (&P_, vb));
-      if (dtype_ == BMFP_R64F)
+      BMFP_CUDA (cudaMalloc (&P_, block ? vb * (size_t) bs : vb)); // block: bs x bs per block row
+      if (block && dtype_ == BMFP_R64F)
+        block_jacobi_kernel<double><<<grid_, kThreads, 0, stream>>> (A->n_rows, bs, A->d_row_ptr, A->d_cols,
+                                                                      (const double *) A->d_vals, (double *) P_);
+      else if (block)
+        block_jacobi_kernel<float><<<grid_, kThreads, 0, stream>>> (A->n_rows, bs, A->d_row_ptr, A->d_cols,
+                                                                     (const float *) A->d_vals, (float *) P_);
+      else if (dtype_ == BMFP_R64F)
         jacobi_kernel<double><<<grid_, kThreads, 0, stream>>> (A->n_rows, bs, A->d_row_ptr, A->d_cols,
                                                                 (const double *) A->d_vals, (double *) P_);
       else
@@ -986,10 +1134,8 @@ int WideEngine::launch_phase (int phase, cudaStream_t s)
         = make_args<double> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, g_, xp_, part_, grid_, state_);
       if (phase == 2 || phase == 4)
         launch_spmv_dispatch<double> (spmv_kind_, phase, a, s);
-      else if (jacobi_)
-        launch_vector_phase<double, true> (phase, a, s);
       else
-        launch_vector_phase<double, false> (phase, a, s);
+        launch_vector_phase<double> (pre_kind_, phase, a, s);
     }
   else
     {
@@ -997,10 +1143,8 @@ int WideEngine::launch_phase (int phase, cudaStream_t s)
         = make_args<float> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, g_, xp_, part_, grid_, state_);
       if (phase == 2 || phase == 4)
         launch_spmv_dispatch<float> (spmv_kind_, phase, a, s);
-      else if (jacobi_)
-        launch_vector_phase<float, true> (phase, a, s);
       else
-        launch_vector_phase<float, false> (phase, a, s);
+        launch_vector_phase<float> (pre_kind_, phase, a, s);
     }
   BMFP_LAUNCH_CHECK ();
   return BMFP_SUCCESS;
@@ -1265,20 +1409,16 @@ int raw_phase (const RawSolve &b, int phase, cudaStream_t s)
       const Args<double> a = raw_args<double> (b);
       if (phase == 2 || phase == 4)
         launch_spmv_dispatch<double> (kind, phase, a, s);
-      else if (b.jacobi)
-        launch_vector_phase<double, true> (phase, a, s);
       else
-        launch_vector_phase<double, false> (phase, a, s);
+        launch_vector_phase<double> (b.jacobi ? kPrePoint : kPreNone, phase, a, s);
     }
   else
     {
       const Args<float> a = raw_args<float> (b);
       if (phase == 2 || phase == 4)
         launch_spmv_dispatch<float> (kind, phase, a, s);
-      else if (b.jacobi)
-        launch_vector_phase<float, true> (phase, a, s);
       else
-        launch_vector_phase<float, false> (phase, a, s);
+        launch_vector_phase<float> (b.jacobi ? kPrePoint : kPreNone, phase, a, s);
     }
   BMFP_LAUNCH_CHECK ();
   return BMFP_SUCCESS;

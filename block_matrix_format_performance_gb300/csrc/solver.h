@@ -54,10 +54,13 @@ struct DevState
   int dslot;
 };
 
-// Replacement threshold on dev / ||r|| (van der Vorst and Ye use sqrt(eps);
-// 1e-3 measured best on the Q4 elasticity family: every grid up to 400x100
-// ends below 1e-10 in b - A x with one to three replacements).
-constexpr double kReplaceThreshold = 1e-3;
+// Replacement threshold on dev / ||r|| (van der Vorst and Ye use sqrt(eps),
+// which replaces tens of times per solve here). With cA's generous bound, a
+// larger threshold places the replacements deeper in the convergence: 1e-2
+// measured best on the Q4 elasticity family (every grid of the uneven batch
+// ends below 1e-10 in b - A x with one or two replacements; 1000x250 takes
+// 4021 iterations, against 4605 with 1e-3 and six replacements).
+constexpr double kReplaceThreshold = 1e-2;
 
 static_assert (offsetof (DevState, done) % 8 == 0 && offsetof (DevState, rep_now) == offsetof (DevState, done) + 4,
                "done and rep_now must form one aligned 8-byte word");
@@ -88,7 +91,8 @@ public:
   WideEngine (const WideEngine &) = delete;
   WideEngine &operator= (const WideEngine &) = delete;
 
-  int init (const bmfp_matrix_s *A, bool jacobi, int chunk, cudaStream_t stream, int ctas_per_sm = 4);
+  // precond: BMFP_PRECOND_NONE, _JACOBI (point) or _BLOCK_JACOBI (bs <= 8).
+  int init (const bmfp_matrix_s *A, int precond, int chunk, cudaStream_t stream, int ctas_per_sm = 4);
   // Residual replacement on (default for FP64 engines) or off (the
   // reference's plain recurrences; FP32 engines always run without it).
   void set_replacement (bool on) { replace_ = on && dtype_ == BMFP_R64F; }
@@ -131,7 +135,8 @@ private:
 
   const bmfp_matrix_s *A_ = nullptr;
   int dtype_ = BMFP_R64F;
-  bool jacobi_ = false;
+  bool jacobi_ = false; // any preconditioner (q, z and P allocated)
+  int pre_kind_ = 0;     // PreKind of the vector phases
   bool replace_ = true;
   bool from_zero_ = true; // the current run started from x = 0
   int64_t n_ = 0;

@@ -372,7 +372,8 @@ int bmfp_solver_create (bmfp_solver_t *out, bmfp_matrix_t A, const bmfp_solver_o
     o = *opts;
   if (o.precision < BMFP_SOLVE_FP64 || o.precision > BMFP_SOLVE_MIXED)
     return fail (BMFP_ERROR_INVALID_VALUE, "invalid precision %d", o.precision);
-  if (o.preconditioner != BMFP_PRECOND_NONE && o.preconditioner != BMFP_PRECOND_JACOBI)
+  if (o.preconditioner != BMFP_PRECOND_NONE && o.preconditioner != BMFP_PRECOND_JACOBI
+      && o.preconditioner != BMFP_PRECOND_BLOCK_JACOBI)
     return fail (BMFP_ERROR_INVALID_VALUE, "invalid preconditioner %d", o.preconditioner);
   if (!(o.tolerance > 0) || o.max_iterations < 0 || o.iterations_per_graph < 1 || o.ctas_per_sm < 1
       || o.ctas_per_sm > 8 || o.inner_stall_iterations < 0)
@@ -391,7 +392,7 @@ int bmfp_solver_create (bmfp_solver_t *out, bmfp_matrix_t A, const bmfp_solver_o
     return fail (BMFP_ERROR_OUT_OF_MEMORY, "host allocation failed");
   sv->opts = o;
   sv->A = A;
-  const bool jac = o.preconditioner == BMFP_PRECOND_JACOBI;
+  const int jac = o.preconditioner;
   int rc = BMFP_SUCCESS;
   const bmfp_matrix_s *A32 = A;
   if (o.precision != BMFP_SOLVE_FP64 && A->dtype == BMFP_R64F)

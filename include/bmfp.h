@@ -271,7 +271,10 @@ enum bmfp_solve_precision
 enum bmfp_preconditioner
 {
   BMFP_PRECOND_NONE = 0,
-  BMFP_PRECOND_JACOBI = 1 /* P = 1/a_ii from the diagonal blocks, bicgstab.cu:201-238 */
+  BMFP_PRECOND_JACOBI = 1, /* P = 1/a_ii from the diagonal blocks, bicgstab.cu:201-238 */
+  BMFP_PRECOND_BLOCK_JACOBI = 2 /* P = inverse of each bs x bs diagonal block (identity where the
+                                   block is missing or singular): the block form of the rule above;
+                                   single-system solver, bs <= 8 */
 };
 
 typedef struct bmfp_solver_options

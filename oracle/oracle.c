@@ -355,9 +355,125 @@ static double orc_dot (int n, const double *a, const double *b)
   return s;
 }
 
+/* M^-1 v: point Jacobi (P), block Jacobi (Minv: n/bs blocks of bs x bs,
+ * row-major) or none. */
+static void orc_apply_precond (int n, int use_precond, const double *P, const double *Minv, int bs,
+                               const double *v, double *out)
+{
+  if (Minv)
+    {
+      for (int br = 0; br < n / bs; br++)
+        for (int r = 0; r < bs; r++)
+          {
+            double acc = 0.0;
+            for (int c = 0; c < bs; c++)
+              acc += Minv[((size_t) br * bs + r) * bs + c] * v[br * bs + c];
+            out[br * bs + r] = acc;
+          }
+      return;
+    }
+  for (int i = 0; i < n; i++)
+    out[i] = use_precond ? P[i] * v[i] : v[i];
+}
+
+static int orc_bicgstab_core (int n, const int *row_ptr, const int *cols, const double *vals,
+                              const double *b, double *x, double eps, int max_iterations,
+                              int use_precond, const double *Minv, int bs, int *iters, double *rel_res);
+
 int orc_bicgstab_f64 (int n, const int *row_ptr, const int *cols, const double *vals,
                       const double *b, double *x, double eps, int max_iterations,
                       int use_precond, int *iters, double *rel_res)
+{
+  return orc_bicgstab_core (n, row_ptr, cols, vals, b, x, eps, max_iterations, use_precond, NULL, 1, iters,
+                            rel_res);
+}
+
+/* Inverse of each bs x bs diagonal block of a CSR matrix whose rows group
+ * into block rows of bs (Gauss-Jordan with partial pivoting), the identity
+ * where the block is zero or a pivot falls below 1e-20 times its largest
+ * entry: the block form of the point rule of bicgstab.cu:201-225. */
+void orc_block_jacobi_f64 (int n, int bs, const int *row_ptr, const int *cols, const double *vals, double *Minv)
+{
+  double *a = (double *) malloc (sizeof (double) * (size_t) bs * bs);
+  for (int br = 0; br < n / bs; br++)
+    {
+      double *inv = Minv + (size_t) br * bs * bs;
+      double amax = 0.0;
+      for (int r = 0; r < bs; r++)
+        {
+          for (int c = 0; c < bs; c++)
+            {
+              a[r * bs + c] = 0.0;
+              inv[r * bs + c] = r == c ? 1.0 : 0.0;
+            }
+          const int row = br * bs + r;
+          for (int e = row_ptr[row]; e < row_ptr[row + 1]; e++)
+            if (cols[e] >= br * bs && cols[e] < (br + 1) * bs)
+              a[r * bs + cols[e] - br * bs] = vals[e];
+        }
+      for (int k = 0; k < bs * bs; k++)
+        amax = fabs (a[k]) > amax ? fabs (a[k]) : amax;
+      int ok = amax > 0.0;
+      for (int c = 0; c < bs && ok; c++)
+        {
+          int piv = c;
+          for (int r = c + 1; r < bs; r++)
+            if (fabs (a[r * bs + c]) > fabs (a[piv * bs + c]))
+              piv = r;
+          if (!(fabs (a[piv * bs + c]) >= 1e-20 * amax))
+            {
+              ok = 0;
+              break;
+            }
+          for (int k = 0; k < bs && piv != c; k++)
+            {
+              double t = a[c * bs + k];
+              a[c * bs + k] = a[piv * bs + k];
+              a[piv * bs + k] = t;
+              t = inv[c * bs + k];
+              inv[c * bs + k] = inv[piv * bs + k];
+              inv[piv * bs + k] = t;
+            }
+          const double d = 1.0 / a[c * bs + c];
+          for (int k = 0; k < bs; k++)
+            {
+              a[c * bs + k] *= d;
+              inv[c * bs + k] *= d;
+            }
+          for (int r = 0; r < bs; r++)
+            if (r != c && a[r * bs + c] != 0.0)
+              {
+                const double f = a[r * bs + c];
+                for (int k = 0; k < bs; k++)
+                  {
+                    a[r * bs + k] -= f * a[c * bs + k];
+                    inv[r * bs + k] -= f * inv[c * bs + k];
+                  }
+              }
+        }
+      if (!ok)
+        for (int k = 0; k < bs * bs; k++)
+          inv[k] = k / bs == k % bs ? 1.0 : 0.0;
+    }
+  free (a);
+}
+
+/* The reference recurrences with block-Jacobi right preconditioning
+ * (q = Minv p, z = Minv s): the block form of bicgstab.cu:454-475. */
+int orc_bicgstab_bj_f64 (int n, int bs, const int *row_ptr, const int *cols, const double *vals,
+                         const double *b, double *x, double eps, int max_iterations, int *iters, double *rel_res)
+{
+  double *Minv = (double *) malloc (sizeof (double) * (size_t) n * bs);
+  orc_block_jacobi_f64 (n, bs, row_ptr, cols, vals, Minv);
+  const int st = orc_bicgstab_core (n, row_ptr, cols, vals, b, x, eps, max_iterations, 1, Minv, bs, iters,
+                                    rel_res);
+  free (Minv);
+  return st;
+}
+
+static int orc_bicgstab_core (int n, const int *row_ptr, const int *cols, const double *vals,
+                              const double *b, double *x, double eps, int max_iterations,
+                              int use_precond, const double *Minv, int bs, int *iters, double *rel_res)
 {
   double *mem = (double *) calloc ((size_t) n * 10, sizeof (double));
   double *r = mem, *rh = mem + n, *p = mem + 2 * n, *v = mem + 3 * n, *h = mem + 4 * n;
@@ -405,8 +521,7 @@ int orc_bicgstab_f64 (int n, const int *row_ptr, const int *cols, const double *
       const double beta = rho / rho_prev * alpha / omega_prev; /* :451 */
       for (int i = 0; i < n; i++)                             /* :452, :286-304 */
         p[i] = r[i] + beta * (p[i] - omega_prev * v[i]);
-      for (int i = 0; i < n; i++)                             /* :454-457 */
-        q[i] = use_precond ? P[i] * p[i] : p[i];
+      orc_apply_precond (n, use_precond, P, Minv, bs, p, q);  /* :454-457 */
       orc_csr_spmv_f64 (n, row_ptr, cols, vals, q, v);        /* :460 */
       const double rh_v = orc_dot (n, rh, v);                 /* :463-466 */
       if (rh_v == 0.0)
@@ -420,8 +535,7 @@ int orc_bicgstab_f64 (int n, const int *row_ptr, const int *cols, const double *
           h[i] = x[i] + alpha * q[i];
           s[i] = r[i] - alpha * v[i];
         }
-      for (int i = 0; i < n; i++)                             /* :472-475 */
-        z[i] = use_precond ? P[i] * s[i] : s[i];
+      orc_apply_precond (n, use_precond, P, Minv, bs, s, z);  /* :472-475 */
       orc_csr_spmv_f64 (n, row_ptr, cols, vals, z, t);        /* :478 */
       const double ts = orc_dot (n, t, s), tt = orc_dot (n, t, t); /* :483-486 */
       if (tt == 0.0)

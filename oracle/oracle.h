@@ -109,6 +109,12 @@ int orc_bicgstab_mt_f64 (int n, const int *row_ptr, const int *cols, const doubl
                          double *x, double eps, int max_iterations, int use_precond, int threads, int *iters,
                          double *rel_res);
 
+/* Block Jacobi: the inverses of the bs x bs diagonal blocks of a CSR matrix
+ * (n rows = n/bs block rows), and BiCGStab with that right preconditioner. */
+void orc_block_jacobi_f64 (int n, int bs, const int *row_ptr, const int *cols, const double *vals, double *Minv);
+int orc_bicgstab_bj_f64 (int n, int bs, const int *row_ptr, const int *cols, const double *vals,
+                         const double *b, double *x, double eps, int max_iterations, int *iters, double *rel_res);
+
 #ifdef __cplusplus
 }
 #endif

@@ -63,6 +63,11 @@ def lib():
                                           ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                           ctypes.POINTER(ctypes.c_double)]
         L.orc_bicgstab_mt_f64.restype = ctypes.c_int
+        L.orc_block_jacobi_f64.argtypes = [ctypes.c_int, ctypes.c_int, _i32p, _i32p, _f64p, _f64p]
+        L.orc_bicgstab_bj_f64.argtypes = [ctypes.c_int, ctypes.c_int, _i32p, _i32p, _f64p, _f64p, _f64p,
+                                          ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                          ctypes.POINTER(ctypes.c_double)]
+        L.orc_bicgstab_bj_f64.restype = ctypes.c_int
         L.orc_band_blocks.argtypes = [ctypes.c_int] * 4
         L.orc_band_blocks.restype = ctypes.c_int
         L.orc_gen_band.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
@@ -208,6 +213,28 @@ def bicgstab(row_ptr, cols, vals, b, eps, max_iterations, use_precond=False):
 # -------------------------------------------- generators (restated specs) ---
 
 _M64 = (1 << 64) - 1
+
+
+def block_jacobi(row_ptr, cols, vals, bs):
+    """Inverses of the bs x bs diagonal blocks of a CSR matrix (identity where
+    singular), shape (n/bs, bs, bs)."""
+    row_ptr = _c(row_ptr, np.int32)
+    n = row_ptr.size - 1
+    out = np.zeros(n * bs, np.float64)
+    lib().orc_block_jacobi_f64(n, bs, row_ptr, _c(cols, np.int32), _c(vals, np.float64), out)
+    return out.reshape(-1, bs, bs)
+
+
+def bicgstab_block_jacobi(row_ptr, cols, vals, bs, b, eps, max_iterations):
+    """bicgstab with block-Jacobi right preconditioning -> (x, status, iters, rel_res)."""
+    row_ptr = _c(row_ptr, np.int32)
+    n = row_ptr.size - 1
+    x = np.zeros(n, np.float64)
+    it = ctypes.c_int(0)
+    rr = ctypes.c_double(0)
+    st = lib().orc_bicgstab_bj_f64(n, bs, row_ptr, _c(cols, np.int32), _c(vals, np.float64), _c(b, np.float64), x,
+                                   float(eps), int(max_iterations), ctypes.byref(it), ctypes.byref(rr))
+    return x, st, it.value, rr.value
 
 
 def bicgstab_mt(row_ptr, cols, vals, b, eps, max_iterations, threads, use_precond=False):

@@ -53,3 +53,21 @@ def test_csr_spmv_into_a_given_buffer(orc):
     for th in (1, 3):
         orc.csr_spmv(rp, c, v, x, threads=th, out=y)
         assert np.array_equal(y, orc.csr_spmv(rp, c, v, x))
+
+
+def test_oracle_block_jacobi_inverse_and_solve(lib, orc):
+    rp, c, v, rhs = bm.gen_q4_elasticity(40, 10)
+    crp, cc, cv = orc.bcsr_to_csr(rp, c, v, 2)
+    M = orc.block_jacobi(crp, cc, cv, 2)
+    D = v.reshape(-1, 2, 2)[np.repeat(np.arange(400), np.diff(rp)) == c]
+    inv = np.linalg.inv(D)
+    assert np.max(np.abs(M - inv)) <= 1e-14 * np.abs(inv).max()
+    x, st, it, rel = orc.bicgstab_block_jacobi(crp, cc, cv, 2, rhs, 1e-10, 20000)
+    y = orc.csr_spmv(crp, cc, cv, x)
+    assert st == 0 and rel < 1e-10 and np.linalg.norm(rhs - y) / np.linalg.norm(rhs) < 1e-9
+    # a zero diagonal block becomes the identity
+    v0 = v.copy().reshape(-1, 2, 2)
+    k = int(np.where((np.repeat(np.arange(400), np.diff(rp)) == c))[0][5])
+    v0[k] = 0.0
+    crp0, cc0, cv0 = orc.bcsr_to_csr(rp, c, v0.reshape(-1), 2)
+    assert np.array_equal(orc.block_jacobi(crp0, cc0, cv0, 2)[5], np.eye(2))
