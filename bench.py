@@ -76,8 +76,8 @@ def parse_args():
     ap.add_argument("--no-fem", action="store_true", help="skip the FEM solves (configs 0 and 2) of the line")
     ap.add_argument("--no-serve", action="store_true", help="skip the served stream (config 4) of the line")
     ap.add_argument("--serve-requests", type=int, default=5000, help="line: requests of the served stream")
-    ap.add_argument("--sustained-requests", type=int, default=None,
-                    help="line: requests of the sustained-rate stream (default: --serve-requests)")
+    ap.add_argument("--sustained-requests", type=int, default=2500,
+                    help="line: requests of the sustained-rate stream (the first of the same stream)")
     ap.add_argument("--serve-precisions", default="mixed",
                     help="line: server precisions at the stated rate (the first also runs at the sustained rate)")
     ap.add_argument("--sustained-factor", type=float, default=0.7,

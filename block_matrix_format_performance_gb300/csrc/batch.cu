@@ -545,7 +545,8 @@ struct Fp64Result
 
 // FP64 BiCGStab with true-residual restarts: from x = 0 (first) or from the
 // current x with its residual in r64. Restarts continue while each one at
-// least halves the true residual (at most 8); each aims at half the one it
+// least halves the true residual (after a breakdown: lowers it at all; at
+// most 8); each aims at half the one it
 // starts from (a restart asked only for the tolerance again, from just above
 // it, moves x by a hair and the true residual with it). Near FP64's
 // attainable accuracy a restart can leave x worse, so the best iterate is
@@ -596,9 +597,11 @@ __device__ Fp64Result fp64_restarted (cg::cluster_group &cl, const TeamSys<doubl
             }
           break;
         }
-      // A restart that did not at least halve the true residual met FP64's
-      // floor (u ||A| |x|| / ||b||): keep its x, stop.
-      const bool halved = rel <= 0.5 * best;
+      // A restart that met its recursive tolerance but did not at least
+      // halve the true residual met FP64's floor (u ||A| |x|| / ||b||):
+      // keep its x, stop. Runs that broke down keep restarting while they
+      // improve at all.
+      const bool halved = rel <= 0.5 * best || o.status != 1;
       best = rel;
       f.rel = rel;
       f.status = o.status;

@@ -39,6 +39,8 @@
 #include "solver.h"
 #include "spmv_core.cuh"
 
+#include <cuda/atomic>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -115,10 +117,12 @@ __device__ __forceinline__ void sum_parts (const double *part, int grid, const i
 #pragma unroll
   for (int k = 0; k < NK; k++)
     acc[k] = 0.0;
+  // __ldcg: the partials were written by other CTAs of this kernel (L2 is
+  // coherent, this SM's L1 need not be)
   for (int i = threadIdx.x; i < grid; i += kThreads)
 #pragma unroll
     for (int k = 0; k < NK; k++)
-      acc[k] += part[ks[k] * grid + i];
+      acc[k] += __ldcg (part + ks[k] * grid + i);
 #pragma unroll
   for (int k = 0; k < NK; k++)
     {
@@ -139,6 +143,28 @@ __device__ __forceinline__ void sum_parts (const double *part, int grid, const i
 #pragma unroll
   for (int k = 0; k < NK; k++)
     out[k] = sh[k];
+}
+
+// True in exactly one CTA of the kernel: the last to finish writing its
+// partials (each CTA's thread 0 wrote them, fences, then counts itself in
+// st->arrive). That CTA resets the counter for the next kernel. No thread
+// waits on another: the last CTA just finds everyone else already done.
+__device__ __forceinline__ bool arrive_last (DevState *st, int grid)
+{
+  __shared__ int sh_last;
+  __syncthreads ();
+  if (threadIdx.x == 0)
+    {
+      // acq_rel at device scope: releases this thread's partial writes to
+      // the CTA that comes last, and acquires everyone's for that CTA.
+      cuda::atomic_ref<unsigned, cuda::thread_scope_device> arrive (st->arrive);
+      const unsigned t = arrive.fetch_add (1u, cuda::memory_order_acq_rel);
+      sh_last = t == (unsigned) grid - 1;
+      if (sh_last)
+        arrive.store (0u, cuda::memory_order_relaxed);
+    }
+  __syncthreads ();
+  return sh_last != 0;
 }
 
 // Reduce per-thread values over the CTA (fixed order) into part[k][blockIdx].
@@ -263,17 +289,80 @@ template <typename T> struct EpiReplace
   }
 };
 
-// phase 2: v = A q, partial (rh, v); in a replacement iteration r = c - A g
-// with partials (rh, r), (r, r) instead (A g lands in t, free until phase 4).
+// The scalars that open an iteration, from the sums of (rh, r), (r, r) and
+// nn: the convergence, limit and breakdown tests, the replacement decision
+// (nn = (g, g) after a replacement or at a run's start, which resets the
+// deviation bound; else (x', x')) and beta. One thread of the last CTA of
+// the kernel that completed the sums runs it. GB300's FP64 pipe is narrow
+// (about 1/58 of FP32): the divides and square roots run once per kernel,
+// not in every CTA.
+__device__ void decide (DevState *st, double rho, double rr, double nn, bool after_rep)
+{
+  if (st->norm_b < 0.0)
+    st->norm_b = sqrt (rr); // ||r0|| of a fresh solve
+  const double nb = st->norm_b;
+  const double omega = st->omega;
+  int status = kStateRunning;
+  double beta = 0.0;
+  const double nr = sqrt (rr);
+  if (nb == 0.0 || nr < st->tol * nb) // gpu/bicgstab.cu:512
+    status = kStateConverged;
+  else if (st->iter >= st->max_iter)
+    status = kStateMaxIter;
+  else if (rho == 0.0 || omega == 0.0 || !isfinite (rho))
+    status = kStateBreakdown;
+  else
+    {
+      beta = rho / st->rho_prev * st->alpha / omega; // gpu/bicgstab.cu:451
+      if (!isfinite (beta))
+        status = kStateBreakdown;
+    }
+  int rep = 0;
+  const double eps = st->eps;
+  if (status == kStateRunning && eps > 0.0)
+    {
+      if (after_rep)
+        st->dev = st->dev0 = eps * (st->cA * sqrt (nn) + nr);
+      else
+        {
+          const double dev = st->dev + eps * (st->cA * sqrt (nn) + nr);
+          rep = st->dev <= kReplaceThreshold * st->nr_prev && dev > kReplaceThreshold * nr && dev > 1.1 * st->dev0;
+          st->dev = dev;
+        }
+      st->nr_prev = nr;
+    }
+  st->rr = rr;
+  if (status != kStateRunning)
+    {
+      st->status = status;
+      *reinterpret_cast<volatile int *> (&st->done) = 1;
+    }
+  else if (rep)
+    {
+      st->rep_now = 1;
+      st->replacements = st->replacements + 1;
+    }
+  else
+    {
+      st->rep_now = 0;
+      st->rho = rho;
+      st->beta = beta;
+    }
+}
+
+// phase 2: v = A q, partial (rh, v); its last CTA derives alpha. In a
+// replacement iteration r = c - A g with partials (rh, r), (r, r) instead
+// (A g lands in t, free until phase 4); phase 5 decides on them.
 template <typename T, class Op>
 __global__ void __launch_bounds__ (kThreads) phase_v (Args<T> a)
 {
-  const int2 f = flags (a.st);
+  DevState *st = a.st;
+  const int2 f = flags (st);
   if (f.x)
     return;
   if (f.y)
     {
-      EpiReplace<T> e{ static_cast<const T *> (a.st->c), a.r, a.rh };
+      EpiReplace<T> e{ static_cast<const T *> (st->c), a.r, a.rh };
       Op::run (a, a.g, a.t, e);
       double vals[2] = { (double) e.rhr, (double) e.rr };
       const int ks[2] = { kRhR, kRR };
@@ -285,13 +374,29 @@ __global__ void __launch_bounds__ (kThreads) phase_v (Args<T> a)
   double vals[1] = { (double) e.acc };
   const int ks[1] = { kRhV };
   store_parts<1> (vals, a.part, a.grid, ks);
+  if (!arrive_last (st, a.grid))
+    return;
+  double sv[1];
+  sum_parts<1> (a.part, a.grid, ks, sv);
+  if (threadIdx.x == 0)
+    {
+      const double alpha = st->rho / sv[0]; // gpu/bicgstab.cu:466
+      if (sv[0] != 0.0 && isfinite (alpha))
+        st->alpha = alpha;
+      else
+        {
+          st->status = kStateBreakdown;
+          *reinterpret_cast<volatile int *> (&st->done) = 1;
+        }
+    }
 }
 
-// phase 4: t = A z, partials (t, s), (t, t)
+// phase 4: t = A z, partials (t, s), (t, t); its last CTA derives omega.
 template <typename T, class Op>
 __global__ void __launch_bounds__ (kThreads) phase_t (Args<T> a)
 {
-  const int2 f = flags (a.st);
+  DevState *st = a.st;
+  const int2 f = flags (st);
   if (f.x || f.y)
     return;
   EpiTS<T> e{ a.s };
@@ -299,6 +404,22 @@ __global__ void __launch_bounds__ (kThreads) phase_t (Args<T> a)
   double vals[2] = { (double) e.ts, (double) e.tt };
   const int ks[2] = { kTS, kTT };
   store_parts<2> (vals, a.part, a.grid, ks);
+  if (!arrive_last (st, a.grid))
+    return;
+  double sv[2];
+  sum_parts<2> (a.part, a.grid, ks, sv);
+  if (threadIdx.x == 0)
+    {
+      const double omega = sv[1] != 0.0 ? sv[0] / sv[1] : 0.0; // :488
+      if (isfinite (omega))
+        st->omega = omega;
+      else
+        {
+          // Leave x' untouched so the run keeps the last finite iterate.
+          st->status = kStateBreakdown;
+          *reinterpret_cast<volatile int *> (&st->done) = 1;
+        }
+    }
 }
 
 // r = b - A x (x given), partials ||r||^2, ||b||^2 — the true residual.
@@ -317,12 +438,43 @@ __global__ void __launch_bounds__ (kThreads)
 
 // Start of a run solving A e = c from e = 0 (ZERO: a fresh solve; else a
 // restart whose c is the true residual of the current x). x itself is not
-// touched until the run ends.
+// touched until the run ends. Its last CTA takes the first decision.
 template <typename T, bool ZERO>
 __global__ void __launch_bounds__ (kThreads)
   start_kernel (Args<T> a, const T *src, double tol, int max_iter, double norm_b, int iter0, double eps,
                 double cA)
 {
+  DevState *st = a.st;
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    {
+      st->rho_prev = 1.0; // gpu/bicgstab.cu:414-420
+      st->alpha = 1.0;
+      st->omega = 1.0;
+      st->rho = 0.0;
+      st->beta = 0.0;
+      st->tol = tol;
+      st->max_iter = max_iter;
+      st->done = 0;
+      st->status = kStateRunning;
+      st->eps = eps;
+      st->cA = cA;
+      st->c = src;
+      st->rep_now = 0;
+      st->replacements = 0;
+      st->dev = st->dev0 = st->nr_prev = 0.0;
+      if (ZERO)
+        {
+          st->iter = 0;
+          st->norm_b = -1.0; // set by the first decision
+        }
+      else
+        {
+          if (norm_b > 0.0)
+            st->norm_b = norm_b;
+          if (iter0 >= 0)
+            st->iter = iter0;
+        }
+    }
   double rr = 0.0;
   GRID_STRIDE (i, a.n)
   {
@@ -338,37 +490,12 @@ __global__ void __launch_bounds__ (kThreads)
   double vals[3] = { rr, rr, 0.0 };
   const int ks[3] = { kRhR, kRR, kGG };
   store_parts<3> (vals, a.part, a.grid, ks);
-  if (blockIdx.x == 0 && threadIdx.x == 0)
-    {
-      DevState *st = a.st;
-      st->rho_prev = 1.0; // gpu/bicgstab.cu:414-420
-      st->alpha = 1.0;
-      st->omega = 1.0;
-      st->rho = 0.0;
-      st->tol = tol;
-      st->max_iter = max_iter;
-      st->done = 0;
-      st->status = kStateRunning;
-      st->eps = eps;
-      st->cA = cA;
-      st->c = src;
-      st->rep_now = 0;
-      st->rep_done = 1; // phase 1 sets the deviation bound from (g, g) = 0 and ||r0||
-      st->replacements = 0;
-      st->dslot = 0;
-      if (ZERO)
-        {
-          st->iter = 0;
-          st->norm_b = -1.0; // set from the first phase-1 sum
-        }
-      else
-        {
-          if (norm_b > 0.0)
-            st->norm_b = norm_b;
-          if (iter0 >= 0)
-            st->iter = iter0;
-        }
-    }
+  if (!arrive_last (st, a.grid))
+    return;
+  double sv[3];
+  sum_parts<3> (a.part, a.grid, ks, sv);
+  if (threadIdx.x == 0)
+    decide (st, sv[0], sv[1], sv[2], true);
 }
 
 // Preconditioner of the vector phases (right preconditioning, q = M^-1 p,
@@ -410,93 +537,18 @@ __device__ __forceinline__ void block_row_apply (const Args<T> &a, int64_t br, T
     }
 }
 
-// phase 1
-// GB300's FP64 pipe is narrow (about 1/58 of FP32), so the scalar divides and
-// square roots run once per CTA (thread 0) and reach the other threads
-// through shared memory instead of being evaluated by every thread.
+// phase 1: p = r + beta (p - omega v) (q = M^-1 p), with beta from the
+// decision that closed the previous kernel; in a replacement iteration the
+// fold g += x', x' = 0 and the partial (g, g) instead.
 template <typename T, int PK>
 __global__ void __launch_bounds__ (kThreads) phase_p (Args<T> a)
 {
   DevState *st = a.st;
-  if (is_done (st))
-    return;
-  // After a replacement (or at a run's start) the third sum is (g, g), which
-  // resets the deviation bound; otherwise it is (x', x').
-  const bool after_rep = st->rep_done != 0;
-  double s[3];
-  const int ks[3] = { kRhR, kRR, after_rep ? kGG : kXX };
-  sum_parts<3> (a.part, a.grid, ks, s);
-  __shared__ double sh_beta, sh_omega;
-  __shared__ int sh_status, sh_rep;
-  if (threadIdx.x == 0)
-    {
-      const double rho = s[0], rr = s[1], nn = s[2];
-      const double nb_state = st->norm_b;
-      const double nb = nb_state < 0.0 ? sqrt (rr) : nb_state;
-      const double omega = st->omega;
-      int status = kStateRunning;
-      double beta = 0.0;
-      if (nb == 0.0 || sqrt (rr) < st->tol * nb) // gpu/bicgstab.cu:512
-        status = kStateConverged;
-      else if (st->iter >= st->max_iter)
-        status = kStateMaxIter;
-      else if (rho == 0.0 || omega == 0.0 || !isfinite (rho))
-        status = kStateBreakdown;
-      else
-        {
-          beta = rho / st->rho_prev * st->alpha / omega; // gpu/bicgstab.cu:451
-          if (!isfinite (beta))
-            status = kStateBreakdown;
-        }
-      int rep = 0;
-      const double eps = st->eps;
-      const int rd = st->dslot, wr = rd ^ 1;
-      double dev = 0.0, dev0 = 0.0;
-      const double nr = sqrt (rr);
-      if (status == kStateRunning && eps > 0.0)
-        {
-          if (after_rep)
-            dev = dev0 = eps * (st->cA * sqrt (nn) + nr);
-          else
-            {
-              dev = st->dev[rd] + eps * (st->cA * sqrt (nn) + nr);
-              dev0 = st->dev0[rd];
-              rep = st->dev[rd] <= kReplaceThreshold * st->nr_prev[rd] && dev > kReplaceThreshold * nr
-                    && dev > 1.1 * dev0;
-            }
-        }
-      if (blockIdx.x == 0)
-        {
-          st->rr = rr;
-          st->dev[wr] = dev;
-          st->dev0[wr] = dev0;
-          st->nr_prev[wr] = nr;
-          if (status != kStateRunning)
-            {
-              st->status = status;
-              *reinterpret_cast<volatile int *> (&st->done) = 1;
-            }
-          else if (rep)
-            {
-              st->rep_now = 1;
-              st->replacements = st->replacements + 1;
-            }
-          else
-            {
-              st->rep_now = 0;
-              st->rho = rho;
-            }
-        }
-      sh_beta = beta;
-      sh_omega = omega;
-      sh_status = status;
-      sh_rep = rep;
-    }
-  __syncthreads ();
-  if (sh_status != kStateRunning)
+  const int2 f = flags (st);
+  if (f.x)
     return;
   const int64_t stride = (int64_t) gridDim.x * blockDim.x;
-  if (sh_rep)
+  if (f.y)
     {
       // Group update: fold the accumulated updates into the base, which
       // phase 2 multiplies by A for the true residual.
@@ -513,7 +565,7 @@ __global__ void __launch_bounds__ (kThreads) phase_p (Args<T> a)
       store_parts<1> (vals, a.part, a.grid, kg);
       return;
     }
-  const T tb = (T) sh_beta, tw = (T) sh_omega;
+  const T tb = (T) st->beta, tw = (T) st->omega;
   if constexpr (PK >= kPreBlock2)
     {
       // block Jacobi: one block row per thread, q = Minv p of the block
@@ -562,34 +614,7 @@ __global__ void __launch_bounds__ (kThreads) phase_s (Args<T> a)
   const int2 f = flags (st);
   if (f.x || f.y)
     return;
-  double s[1];
-  const int ks[1] = { kRhV };
-  sum_parts<1> (a.part, a.grid, ks, s);
-  __shared__ double sh_alpha;
-  if (threadIdx.x == 0)
-    {
-      const double alpha = st->rho / s[0]; // gpu/bicgstab.cu:466
-      const bool ok = s[0] != 0.0 && isfinite (alpha);
-      sh_alpha = ok ? alpha : NAN;
-      if (blockIdx.x == 0)
-        {
-          if (ok)
-            {
-              st->alpha = alpha;
-              if (st->norm_b < 0.0)
-                st->norm_b = sqrt (st->rr);
-            }
-          else
-            {
-              st->status = kStateBreakdown;
-              *reinterpret_cast<volatile int *> (&st->done) = 1;
-            }
-        }
-    }
-  __syncthreads ();
-  const double alpha = sh_alpha;
-  if (!isfinite (alpha))
-    return;
+  const double alpha = st->alpha; // phase 2's last CTA
   const T ta = (T) alpha;
   const int64_t stride = (int64_t) gridDim.x * blockDim.x;
   if constexpr (PK >= kPreBlock2)
@@ -627,7 +652,9 @@ __global__ void __launch_bounds__ (kThreads) phase_s (Args<T> a)
     }
 }
 
-// phase 5
+// phase 5: x' += alpha q + omega z, r = s - omega t, partials (rh, r),
+// (r, r), (x', x'); its last CTA takes the decision that opens the next
+// iteration.
 template <typename T, int PK>
 __global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
 {
@@ -637,35 +664,18 @@ __global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
     return;
   if (f.y)
     {
-      // r, (rh, r) and (r, r) came from phase 2; nothing else moves.
-      if (blockIdx.x == 0 && threadIdx.x == 0)
-        {
-          st->rep_done = 1;
-          st->dslot = st->dslot ^ 1;
-        }
+      // r, (rh, r) and (r, r) came from phase 2 and (g, g) from phase 1:
+      // the last CTA takes the decision that opens the next iteration.
+      if (!arrive_last (st, a.grid))
+        return;
+      double sv[3];
+      const int ks[3] = { kRhR, kRR, kGG };
+      sum_parts<3> (a.part, a.grid, ks, sv);
+      if (threadIdx.x == 0)
+        decide (st, sv[0], sv[1], sv[2], true);
       return;
     }
-  double s[2];
-  const int ks[2] = { kTS, kTT };
-  sum_parts<2> (a.part, a.grid, ks, s);
-  __shared__ double sh_alpha, sh_omega;
-  if (threadIdx.x == 0)
-    {
-      const double omega = s[1] != 0.0 ? s[0] / s[1] : 0.0; // :488
-      sh_alpha = st->alpha;
-      sh_omega = isfinite (omega) ? omega : NAN;
-      if (blockIdx.x == 0 && !isfinite (omega))
-        {
-          // Leave x' untouched so the run keeps the last finite iterate.
-          st->status = kStateBreakdown;
-          *reinterpret_cast<volatile int *> (&st->done) = 1;
-        }
-    }
-  __syncthreads ();
-  const double omega = sh_omega;
-  if (!isfinite (omega))
-    return;
-  const T ta = (T) sh_alpha, tw = (T) omega;
+  const T ta = (T) st->alpha, tw = (T) st->omega;
   // (x', x') feeds the replacement bound only: skipped (0) when it is off.
   const bool track = st->eps > 0.0;
   T rhr = 0, rr = 0, xx = 0;
@@ -716,13 +726,15 @@ __global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
   double vals[3] = { (double) rhr, (double) rr, (double) xx };
   const int kk[3] = { kRhR, kRR, kXX };
   store_parts<3> (vals, a.part, a.grid, kk);
-  if (blockIdx.x == 0 && threadIdx.x == 0)
+  if (!arrive_last (st, a.grid))
+    return;
+  double sv[3];
+  sum_parts<3> (a.part, a.grid, kk, sv);
+  if (threadIdx.x == 0)
     {
-      st->omega = omega;
       st->rho_prev = st->rho;
       st->iter = st->iter + 1;
-      st->rep_done = 0;
-      st->dslot = st->dslot ^ 1;
+      decide (st, sv[0], sv[1], sv[2], false);
     }
 }
 

@@ -10,8 +10,13 @@
 
 namespace bmfp
 {
-// Device-resident scalars of one BiCGStab solve. Every phase kernel reads
-// only fields written by earlier kernels, so no kernel races with itself.
+// Device-resident scalars of one BiCGStab solve. Each kernel that completes
+// a set of dot products (start, phase 2, phase 4, phase 5) has its last CTA
+// to finish sum every CTA's partials, in a fixed order, and derive the
+// scalars the next phases read (alpha, omega, or beta and the tests that
+// open an iteration); the other kernels only read them. So each scalar is
+// computed once per kernel, by one thread, and no kernel reads a field it
+// writes itself.
 //
 // Residual replacement (H. A. van der Vorst and Q. Ye, "Residual replacement
 // strategies for Krylov subspace iterative methods for the convergence of
@@ -27,31 +32,30 @@ namespace bmfp
 // tolerance in b - A x as well.
 struct DevState
 {
-  double rho;      // (rh, r) of the current iteration (phase 1)
-  double rho_prev; // previous iteration's rho (phase 5)
-  double alpha;    // phase 3
-  double omega;    // phase 5
-  double norm_b;   // ||r0|| (phase 1, first iteration)
-  double rr;       // last (r, r) seen by phase 1
+  double rho;      // (rh, r) of the current iteration
+  double rho_prev; // previous iteration's rho
+  double alpha;    // set by phase 2's last CTA
+  double omega;    // set by phase 4's last CTA
+  double beta;     // of the next p update
+  double norm_b;   // ||r0|| (set by the first decision)
+  double rr;       // last (r, r)
   double tol;      // stop when sqrt(rr) / norm_b < tol
   double eps;      // unit roundoff of the working precision; 0 = no replacement
   double cA;       // max entries per scalar row * max absolute row sum
-  // Deviation bound since the last replacement, its value at that
-  // replacement, and ||r|| of the previous iteration: phase 1 reads slot
-  // dslot and writes slot dslot ^ 1 (other CTAs of phase 1 still read the
-  // old values), phase 5 flips dslot.
-  double dev[2], dev0[2], nr_prev[2];
+  double dev;      // deviation bound since the last replacement
+  double dev0;     // its value at the last replacement
+  double nr_prev;  // ||r|| at the previous decision
   const void *c;   // right-hand side of the run (b, or a restart's residual)
   // done and rep_now side by side (8-byte aligned): every phase reads both
   // with one load at its start.
-  int done;        // set by phase 1; every kernel returns early once set
-  int rep_now;     // phase 1 chose to replace r this iteration (read by phases 2-5)
-  int iter;        // iterations completed (phase 5)
+  int done;        // set by a decision; every kernel returns early once set
+  int rep_now;     // this iteration replaces r by the true residual
+  int iter;        // iterations completed
   int max_iter;
   int status;      // 0 running, 1 converged, 2 iteration limit, 3 breakdown
-  int rep_done;    // the iteration phase 5 just closed was a replacement (read by phase 1)
   int replacements;
-  int dslot;
+  unsigned arrive; // CTAs of the running kernel that have written their partials
+  int pad;
 };
 
 // Replacement threshold on dev / ||r|| (van der Vorst and Ye use sqrt(eps),

@@ -63,8 +63,9 @@ int run_keep_best (WideEngine &e, void *d_snap, DevState *st, cudaStream_t s, in
 }
 
 // Restart loop shared by the plain and the mixed solves: verify b - A x,
-// restart from the true residual while each restart at least halves it (at
-// most 8 times), and keep the best iterate: near the attainable accuracy of the
+// restart from the true residual while each restart at least halves it (or,
+// after a breakdown, lowers it at all; at most 8 times), and keep the best
+// iterate: near the attainable accuracy of the
 // working precision a restart can leave x worse (the more so the lower it
 // aims: a tenth of its starting residual measured worse than half), and then
 // x is restored.
@@ -95,9 +96,11 @@ int finish_with_restarts (WideEngine &e, const void *d_b, void *d_r, void *d_xbe
             best = rel;
           break;
         }
-      // A restart that did not at least halve the true residual met the
-      // working precision's floor (u ||A| |x|| / ||b||): keep its x, stop.
-      const bool halved = rel <= 0.5 * best;
+      // A restart that met its recursive tolerance but did not at least
+      // halve the true residual met the working precision's floor
+      // (u ||A| |x|| / ||b||): keep its x, stop. Runs that broke down keep
+      // restarting while they improve at all.
+      const bool halved = rel <= 0.5 * best || st.status != kStateConverged;
       best = rel;
       best_st = st;
       // A breakdown also restarts (a fresh shadow residual is the usual

@@ -2,10 +2,11 @@
 (gpu/bicgstab.cu:387-513) and an independent FP64 direct solve.
 
 Bars: true relative residual ||b - A x|| / ||b|| below the tolerance, error
-against the direct solve reported and bounded, iteration counts within 25 %
-(+10) of the oracle's (the dot products sum in a different order; BiCGStab's
-erratic residual history on these operators turns that into a different
-iteration count, most visibly with Jacobi), and bitwise repeatability.
+against the direct solve reported and bounded, iteration counts of the plain
+recurrences (the oracle's algorithm) within 25 % (+10) of the oracle's (the
+dot products sum in a different order; BiCGStab's erratic residual history on
+these operators turns that into a different iteration count, most visibly
+with Jacobi), and bitwise repeatability.
 """
 import numpy as np
 import pytest
@@ -62,8 +63,13 @@ def test_fp64_q4_elasticity_matches_oracle(lib, orc, cuda, grid, precond):
     assert err < 1e-5, err  # reported: forward error bounded by cond(A) * residual
     crp, cc, cv = orc.bcsr_to_csr(rp, c, v, 2)
     xo, st, it_o, _ = orc.bicgstab(crp, cc, cv, rhs, 1e-10, 50000, precond == "jacobi")
-    it_first = info["iterations"]
-    assert abs(it_first - it_o) <= 0.25 * it_o + 10 + 50 * info["restarts"], (it_first, it_o, info)
+    # Iteration counts compare the oracle's own algorithm: the plain
+    # recurrences stopped on the recursive residual (no replacement, no
+    # restart); the dot products still sum in another order.
+    _, plain = bm.Solver(A, "fp64", tol=1e-10, max_iters=50000, preconditioner=precond,
+                         check_true_residual=False).solve_host(rhs)
+    assert plain["replacements"] == 0 and plain["restarts"] == 0
+    assert abs(plain["iterations"] - it_o) <= 0.25 * it_o + 10, (plain, it_o, info)
     s.close(), A.close()
 
 
