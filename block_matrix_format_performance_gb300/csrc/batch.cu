@@ -309,13 +309,14 @@ struct Scal
 template <typename T, int OP, bool RR = false>
 __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, const T *rhs, T *x, bool zero_x,
                                    double tol, int max_it, double norm_ref, T *snap = nullptr, int stall = 0,
-                                   const T *bt = nullptr, T *xp = nullptr, double cA = 0.0, int *reps = nullptr)
+                                   const T *bt = nullptr, T *xp = nullptr, double cA = 0.0, int *reps = nullptr,
+                                   bool new_shadow = false)
 {
   using Op = TeamOp<T, OP>;
   const TeamIdx ix = team_index<Op::G> (cl);
   __shared__ Scal sc;
   SolveOut o;
-  double rr0 = 0.0;
+  double rr0 = 0.0, rhr0 = 0.0;
   for (int64_t i = ix.elem0; i < S.n; i += ix.elem_stride)
     {
       const T ri = rhs[i];
@@ -323,22 +324,25 @@ __device__ SolveOut team_bicgstab (cg::cluster_group &cl, const TeamSys<T> &S, c
         x[i] = 0;
       if (RR)
         xp[i] = 0;
+      // after a breakdown: a perturbed shadow residual (shadow_factor)
+      const T hi = new_shadow ? (T) (ri * shadow_factor (i)) : ri;
       S.r[i] = ri;
-      S.rh[i] = ri;
+      S.rh[i] = hi;
       S.p[i] = 0;
       S.v[i] = 0;
       rr0 = fma ((double) ri, (double) ri, rr0);
+      rhr0 = fma ((double) hi, (double) ri, rhr0);
     }
-  double in1[2] = { rr0, 0.0 }, out1[2];
+  double in1[3] = { rr0, 0.0, rhr0 }, out1[3];
   if (RR && !zero_x)
     for (int64_t i = ix.elem0; i < S.n; i += ix.elem_stride)
       in1[1] = fma ((double) x[i], (double) x[i], in1[1]);
-  team_sum<2> (cl, in1, out1);
+  team_sum<3> (cl, in1, out1);
   if (threadIdx.x == 0)
     sc.a = norm_ref > 0.0 ? norm_ref : sqrt (out1[0]);
   __syncthreads ();
   const double nb = sc.a;
-  double rho = out1[0], rr = out1[0]; // rh == r at the start
+  double rho = out1[2], rr = out1[0]; // rho = (rh, r0), rh = r0 unless perturbed
   double mark_rr = out1[0];           // best (r, r) at the last halving
   int mark_it = 0;
   double rho_prev = 1.0, alpha = 1.0, omega = 1.0;
@@ -564,11 +568,13 @@ __device__ Fp64Result fp64_restarted (cg::cluster_group &cl, const TeamSys<doubl
   Fp64Result f;
   double best = INFINITY;
   double target = P.tol; // a restart aims at half the true residual it starts from
+  bool shadow = false;   // restart after a breakdown: perturbed shadow residual
   for (;;)
     {
       const SolveOut o = team_bicgstab<double, OP, true> (cl, S64, first ? D.b : r64, D.x, first, target,
                                                           budget - f.iters, norm_b, snap, 0, D.b, xp, cA,
-                                                          &f.replacements);
+                                                          &f.replacements, shadow);
+      shadow = o.status == 3;
       f.iters += o.iters;
       double rr, bb;
       team_residual<OP> (cl, S64, D.b, D.x, r64, rr, bb);

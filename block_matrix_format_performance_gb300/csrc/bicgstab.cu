@@ -442,7 +442,7 @@ __global__ void __launch_bounds__ (kThreads)
 template <typename T, bool ZERO>
 __global__ void __launch_bounds__ (kThreads)
   start_kernel (Args<T> a, const T *src, double tol, int max_iter, double norm_b, int iter0, double eps,
-                double cA)
+                double cA, int new_shadow)
 {
   DevState *st = a.st;
   if (blockIdx.x == 0 && threadIdx.x == 0)
@@ -475,19 +475,21 @@ __global__ void __launch_bounds__ (kThreads)
             st->iter = iter0;
         }
     }
-  double rr = 0.0;
+  double rr = 0.0, rhr = 0.0;
   GRID_STRIDE (i, a.n)
   {
     const T ri = src[i];
+    const T hi = new_shadow ? (T) (ri * shadow_factor (i)) : ri;
     a.r[i] = ri;
-    a.rh[i] = ri;
+    a.rh[i] = hi;
     a.p[i] = 0;
     a.v[i] = 0;
     a.g[i] = 0;
     a.xp[i] = 0;
     rr = fma ((double) ri, (double) ri, rr);
+    rhr = fma ((double) hi, (double) ri, rhr);
   }
-  double vals[3] = { rr, rr, 0.0 };
+  double vals[3] = { rhr, rr, 0.0 };
   const int ks[3] = { kRhR, kRR, kGG };
   store_parts<3> (vals, a.part, a.grid, ks);
   if (!arrive_last (st, a.grid))
@@ -1186,7 +1188,8 @@ int WideEngine::capture (cudaStream_t s)
   return BMFP_SUCCESS;
 }
 
-int WideEngine::start (bool zero, const void *c, double tol, int max_iter, double norm_b, int iter0, cudaStream_t s)
+int WideEngine::start (bool zero, const void *c, double tol, int max_iter, double norm_b, int iter0, bool new_shadow,
+                        cudaStream_t s)
 {
   void *q = jacobi_ ? q_ : p_;
   void *z = jacobi_ ? z_ : s_;
@@ -1199,10 +1202,10 @@ int WideEngine::start (bool zero, const void *c, double tol, int max_iter, doubl
         = make_args<double> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, g_, xp_, part_, grid_, state_);
       if (zero)
         start_kernel<double, true><<<grid_, kThreads, 0, s>>> (a, (const double *) c, tol, max_iter, norm_b, iter0,
-                                                                eps, cA_);
+                                                                eps, cA_, new_shadow ? 1 : 0);
       else
         start_kernel<double, false><<<grid_, kThreads, 0, s>>> (a, (const double *) c, tol, max_iter, norm_b,
-                                                                 iter0, eps, cA_);
+                                                                 iter0, eps, cA_, new_shadow ? 1 : 0);
     }
   else
     {
@@ -1210,10 +1213,10 @@ int WideEngine::start (bool zero, const void *c, double tol, int max_iter, doubl
         = make_args<float> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, g_, xp_, part_, grid_, state_);
       if (zero)
         start_kernel<float, true><<<grid_, kThreads, 0, s>>> (a, (const float *) c, tol, max_iter, norm_b, iter0,
-                                                               eps, cA_);
+                                                               eps, cA_, new_shadow ? 1 : 0);
       else
         start_kernel<float, false><<<grid_, kThreads, 0, s>>> (a, (const float *) c, tol, max_iter, norm_b, iter0,
-                                                                eps, cA_);
+                                                                eps, cA_, new_shadow ? 1 : 0);
     }
   BMFP_LAUNCH_CHECK ();
   return BMFP_SUCCESS;
@@ -1221,13 +1224,13 @@ int WideEngine::start (bool zero, const void *c, double tol, int max_iter, doubl
 
 int WideEngine::start_zero (const void *d_b, double tol, int max_iter, cudaStream_t s)
 {
-  return start (true, d_b, tol, max_iter, -1.0, 0, s);
+  return start (true, d_b, tol, max_iter, -1.0, 0, false, s);
 }
 
 int WideEngine::start_residual (const void *d_r, double tol, int max_iter_total, double norm_b,
-                                cudaStream_t s, int iter0)
+                                cudaStream_t s, int iter0, bool new_shadow)
 {
-  return start (false, d_r, tol, max_iter_total, norm_b, iter0, s);
+  return start (false, d_r, tol, max_iter_total, norm_b, iter0, new_shadow, s);
 }
 
 namespace
@@ -1405,10 +1408,10 @@ int raw_start (const RawSolve &b, const void *d_rhs, double tol, int max_iter, c
 {
   if (b.A.dtype == BMFP_R64F)
     start_kernel<double, true><<<b.grid, kThreads, 0, s>>> (raw_args<double> (b), (const double *) d_rhs,
-                                                            tol, max_iter, -1.0, 0, 0.0, 0.0);
+                                                            tol, max_iter, -1.0, 0, 0.0, 0.0, 0);
   else
     start_kernel<float, true><<<b.grid, kThreads, 0, s>>> (raw_args<float> (b), (const float *) d_rhs,
-                                                           tol, max_iter, -1.0, 0, 0.0, 0.0);
+                                                           tol, max_iter, -1.0, 0, 0.0, 0.0, 0);
   BMFP_LAUNCH_CHECK ();
   return BMFP_SUCCESS;
 }

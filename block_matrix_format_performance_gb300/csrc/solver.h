@@ -109,8 +109,10 @@ public:
   // never ran start_zero has none); norm_b <= 0 keeps the previous one.
   // iter0 >= 0 restarts the iteration count there (a new solve on an engine
   // whose last run belonged to an earlier one); -1 keeps counting.
+  // new_shadow: the shadow residual is r0 perturbed elementwise
+  // (shadow_factor) instead of r0 itself, for a restart after a breakdown.
   int start_residual (const void *d_r, double tol, int max_iter_total, double norm_b,
-                      cudaStream_t stream, int iter0 = -1);
+                      cudaStream_t stream, int iter0 = -1, bool new_shadow = false);
   // Runs graphs until the device sets done, then writes the run's result
   // into x; returns the final state. With d_snapshot, the run's iterate is
   // copied there each time the recursive residual has fallen 4x below the
@@ -135,7 +137,8 @@ public:
 private:
   int capture (cudaStream_t stream);
   int launch_phase (int phase, cudaStream_t stream);
-  int start (bool zero, const void *c, double tol, int max_iter, double norm_b, int iter0, cudaStream_t s);
+  int start (bool zero, const void *c, double tol, int max_iter, double norm_b, int iter0, bool new_shadow,
+             cudaStream_t s);
 
   const bmfp_matrix_s *A_ = nullptr;
   int dtype_ = BMFP_R64F;
@@ -185,6 +188,21 @@ int raw_start (const RawSolve &b, const void *d_rhs, double tol, int max_iter, c
 int raw_phase (const RawSolve &b, int phase, cudaStream_t stream);
 // x = g + xp: the run's result into the caller's x (after the last phase).
 int raw_finish (const RawSolve &b, cudaStream_t stream);
+
+// Factor in [0.5, 1.5) of element i of a shadow residual after a breakdown:
+// rh_i = r_i * shadow_factor (i). BiCGStab breaks down when (rh, r) or
+// (rh, v) vanishes; a restart from the true residual with rh = r can meet the
+// same breakdown again, so it perturbs rh by a fixed hash of the index
+// (SplitMix64 finaliser), staying correlated with r ((rh, r) > 0) but no
+// longer parallel to it. Deterministic: the same solve gives the same bits.
+__host__ __device__ inline double shadow_factor (int64_t i)
+{
+  uint64_t z = (uint64_t) i * 0x9E3779B97F4A7C15ull + 0x5DEECE66Dull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return 0.5 + (double) (z >> 11) * (1.0 / 9007199254740992.0);
+}
 
 // Elementwise helpers used by the refinement loop (vector_ops.cu).
 int axpy_scaled_convert (int dst_dtype, int src_dtype, int64_t n, double a, const void *src,

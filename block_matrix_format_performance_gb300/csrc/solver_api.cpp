@@ -113,8 +113,10 @@ int finish_with_restarts (WideEngine &e, const void *d_b, void *d_r, void *d_xbe
       // Aim at half the true residual the restart starts from: asked only
       // for the tolerance again, from just above it, a restart moves x by a
       // hair and the true residual with it.
+      // After a breakdown the restart takes a perturbed shadow residual
+      // (the same one would likely break down again).
       rc = e.start_residual (d_r, std::min (o.tolerance, 0.5 * rel), iter_budget,
-                             norm_b > 0 ? norm_b : std::sqrt (bb), s);
+                             norm_b > 0 ? norm_b : std::sqrt (bb), s, -1, st.status == kStateBreakdown);
       if (rc == BMFP_SUCCESS)
         rc = run_keep_best (e, d_snap, &st, s, reps);
       if (rc != BMFP_SUCCESS)

@@ -342,3 +342,31 @@ def test_block_jacobi_limits(lib, cuda):
     m = bm.Matrix.from_bcsr(rp, c, v, 2)
     with pytest.raises(bm.BmfpError):
         bm.Batch([m], "fp64", preconditioner=bm.PRECOND_BLOCK_JACOBI)
+
+
+def test_breakdown_restart_takes_a_new_shadow_residual(lib, cuda):
+    """Request 3331 of the 5000-request serving stream (1000x250 grid, random
+    load) on the whole-GPU solver as the server's wide lanes run it (one CTA
+    per SM): BiCGStab breaks down there, and restarts from the true residual
+    with the same shadow vector (rh = r) broke down again, ending at 2.3e-6.
+    A restart after a breakdown now takes a perturbed shadow residual."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    _, grids = bench.serve_stream(5000, 2000.0)
+    rng = np.random.default_rng(7)
+    b = None
+    for nx, ny in grids[:3332]:
+        b = rng.uniform(-1, 1, 2 * nx * ny)
+        b.reshape(ny, nx, 2)[:, 0, :] = 0.0
+    assert grids[3331] == (1000, 250)
+    rp, c, v, _ = bm.gen_q4_elasticity(1000, 250)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    x, info = bm.Solver(A, "fp64", tol=1e-10, ctas_per_sm=1).solve_host(b)
+    K = bcsr_dense_csr(rp, c, v, 2)
+    rel = np.linalg.norm(b - K @ x) / np.linalg.norm(b)
+    floor = bench.fp64_floor(rp, c, v, 2, x, b)
+    assert info["status"] != bm.ERROR_BREAKDOWN, info
+    assert rel < max(1e-10, 2 * floor), (rel, floor, info)
+    A.close()
