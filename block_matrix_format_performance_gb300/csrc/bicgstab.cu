@@ -167,28 +167,36 @@ __device__ __forceinline__ bool arrive_last (DevState *st, int grid)
   return sh_last != 0;
 }
 
-// Reduce per-thread values over the CTA (fixed order) into part[k][blockIdx].
+// Reduce per-thread values over the CTA (fixed order) into part[k][blockIdx]:
+// a tree through shared memory (128, 64, 32 threads add pairs) and one warp
+// butterfly for the last 32. Each warp-wide FP64 add costs GB300's narrow
+// FP64 pipe the same whatever the number of useful lanes: the tree takes
+// 12 warp adds per value and CTA, a butterfly in every warp took 45.
 template <int NK>
 __device__ __forceinline__ void store_parts (double (&v)[NK], double *part, int grid,
                                              const int (&ks)[NK])
 {
-  __shared__ double sh[NK][kWarps];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __shared__ double sh[NK][kThreads];
+  const int t = threadIdx.x;
 #pragma unroll
   for (int k = 0; k < NK; k++)
-    {
-      const double s = warp_sum (v[k]);
-      if (lane == 0)
-        sh[k][w] = s;
-    }
+    sh[k][t] = v[k];
   __syncthreads ();
-  if (threadIdx.x < 32)
+#pragma unroll
+  for (int h = kThreads / 2; h >= 32; h >>= 1)
+    {
+      if (t < h)
+#pragma unroll
+        for (int k = 0; k < NK; k++)
+          sh[k][t] += sh[k][t + h];
+      __syncthreads ();
+    }
+  if (t < 32)
 #pragma unroll
     for (int k = 0; k < NK; k++)
       {
-        double a = lane < kWarps ? sh[k][lane] : 0.0;
-        a = warp_sum (a);
-        if (lane == 0)
+        const double a = warp_sum (sh[k][t]);
+        if (t == 0)
           part[ks[k] * grid + blockIdx.x] = a;
       }
 }
