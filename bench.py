@@ -288,7 +288,10 @@ def read_floor_us(byte_counts, flush, stream, reps=20):
 
 def committed_traffic(kernel_key):
     """dram bytes per launch of the dominant kernel from the committed ncu
-    summary (profiles/*.md line `traffic <key>: <bytes>`), or None."""
+    summary (profiles/*.md line `traffic <key>: <bytes>`), or None. The key
+    names the case and the lane mapping the capture ran (`..._lanes<L>`): a
+    run that picks another mapping finds no line and reports null rather than
+    another kernel's bytes."""
     pdir = os.path.join(ROOT, "profiles")
     if not os.path.isdir(pdir):
         return None
@@ -397,7 +400,7 @@ def run_ours(args):
     dom_ms = per_case_ms[dom] / args.steps
     hbm, peak_kind = peaks()
     achieved = dcs["bytes"] / (dom_ms * 1e-3) / 1e9
-    dom_key = f"bcsr_native_bs{dcs['bs']}_{dcs['tag']}"
+    dom_key = f"bcsr_native_bs{dcs['bs']}_{dcs['tag']}_lanes{dcs['lanes']}"
     traffic = committed_traffic(dom_key)
     fp64_bound = None
     if dcs["tag"] == "f64":

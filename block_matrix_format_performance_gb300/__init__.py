@@ -368,6 +368,8 @@ class Matrix:
 
 SOLVE_FP64, SOLVE_FP32, SOLVE_MIXED = 0, 1, 2
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_BLOCK_JACOBI = 0, 1, 2
+LAUNCH_AUTO, LAUNCH_GRAPH, LAUNCH_PERSISTENT = 0, 1, 2
+_LAUNCH_MODES = {"auto": LAUNCH_AUTO, "graph": LAUNCH_GRAPH, "persistent": LAUNCH_PERSISTENT}
 _PRECISIONS = {"fp64": SOLVE_FP64, "fp32": SOLVE_FP32, "mixed": SOLVE_MIXED}
 
 
@@ -383,6 +385,8 @@ def solver_options(base=None, **kw) -> SolverOptions:
             v = _PRECISIONS[v]
         if k == "preconditioner" and isinstance(v, str):
             v = {"none": PRECOND_NONE, "jacobi": PRECOND_JACOBI, "block_jacobi": PRECOND_BLOCK_JACOBI}[v]
+        if k == "launch_mode" and isinstance(v, str):
+            v = _LAUNCH_MODES[v]
         setattr(o, k, int(v) if isinstance(v, bool) else v)
     return o
 

@@ -100,7 +100,7 @@ class SolverOptions(ctypes.Structure):
                 ("max_iterations", c_int), ("check_true_residual", c_int), ("inner_tolerance", c_double),
                 ("inner_max_iterations", c_int), ("max_refinements", c_int), ("fallback_fp64", c_int),
                 ("iterations_per_graph", c_int), ("ctas_per_sm", c_int), ("inner_stall_iterations", c_int),
-                ("residual_replacement", c_int)]
+                ("residual_replacement", c_int), ("launch_mode", c_int)]
 
 
 class SolveInfo(ctypes.Structure):

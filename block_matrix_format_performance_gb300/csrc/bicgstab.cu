@@ -207,7 +207,7 @@ __device__ __forceinline__ void store_parts (double (&v)[NK], double *part, int 
 
 // ------------------------------------------------------------ SpMV phases
 
-template <typename T, int BS, int G> struct FlatOp
+template <typename T, int BS, int G, class XL = dev::XNc> struct FlatOp
 {
   template <class Epi>
   __device__ static void run (const Args<T> &a, const T *x, T *y, Epi &e)
@@ -215,11 +215,11 @@ template <typename T, int BS, int G> struct FlatOp
     const int64_t group = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) / G;
     const int64_t ng = (int64_t) gridDim.x * blockDim.x / G;
     for (int64_t row = group; row < a.nbr; row += ng)
-      core::flat_row<T, BS, G, 4> ((int) row, a.rp, a.cols, a.vals, x, y, e);
+      core::flat_row<T, BS, G, 4, XL> ((int) row, a.rp, a.cols, a.vals, x, y, e);
   }
 };
 
-template <typename T, int BSC> struct TprOp
+template <typename T, int BSC, class XL = dev::XNc> struct TprOp
 {
   template <class Epi>
   __device__ static void run (const Args<T> &a, const T *x, T *y, Epi &e)
@@ -227,11 +227,11 @@ template <typename T, int BSC> struct TprOp
     const int64_t warp = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = (int64_t) gridDim.x * blockDim.x >> 5;
     for (int64_t row = warp; row < a.nbr; row += nw)
-      core::tpr_row<T, BSC> ((int) row, a.bs, a.rp, a.cols, a.vals, x, y, e);
+      core::tpr_row<T, BSC, XL> ((int) row, a.bs, a.rp, a.cols, a.vals, x, y, e);
   }
 };
 
-template <typename T, int G> struct CsrOp
+template <typename T, int G, class XL = dev::XNc> struct CsrOp
 {
   template <class Epi>
   __device__ static void run (const Args<T> &a, const T *x, T *y, Epi &e)
@@ -239,7 +239,7 @@ template <typename T, int G> struct CsrOp
     const int64_t group = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) / G;
     const int64_t ng = (int64_t) gridDim.x * blockDim.x / G;
     for (int64_t row = group; row < a.nbr; row += ng)
-      core::csr_row<T, G> ((int) row, a.rp, a.cols, a.vals, x, y, e);
+      core::csr_row<T, G, XL> ((int) row, a.rp, a.cols, a.vals, x, y, e);
   }
 };
 
@@ -358,19 +358,21 @@ __device__ void decide (DevState *st, double rho, double rr, double nn, bool aft
     }
 }
 
-// phase 2: v = A q, partial (rh, v); its last CTA derives alpha. In a
-// replacement iteration r = c - A g with partials (rh, r), (r, r) instead
-// (A g lands in t, free until phase 4); phase 5 decides on them.
-template <typename T, class Op>
-__global__ void __launch_bounds__ (kThreads) phase_v (Args<T> a)
+// Each phase is a body, run by every CTA, and (for phases that end in a dot
+// product) a tail that turns the grid's partial sums into the next scalars.
+// The phase kernels of the iteration graph run the tail in the last CTA to
+// finish (arrive_last) on the device state in global memory; the persistent
+// iteration kernel runs it in every CTA, on a copy of the state in shared
+// memory, after a grid barrier. Both sum the partials in the same order, so
+// both give the same bits.
+
+// phase 2: v = A q, partial (rh, v). In a replacement iteration r = c - A g
+// with partials (rh, r), (r, r) instead (A g lands in t, free until phase 4).
+template <typename T, class Op> __device__ __forceinline__ void body_v (const Args<T> &a, const DevState *sc, bool rep)
 {
-  DevState *st = a.st;
-  const int2 f = flags (st);
-  if (f.x)
-    return;
-  if (f.y)
+  if (rep)
     {
-      EpiReplace<T> e{ static_cast<const T *> (st->c), a.r, a.rh };
+      EpiReplace<T> e{ static_cast<const T *> (sc->c), a.r, a.rh };
       Op::run (a, a.g, a.t, e);
       double vals[2] = { (double) e.rhr, (double) e.rr };
       const int ks[2] = { kRhR, kRR };
@@ -382,10 +384,14 @@ __global__ void __launch_bounds__ (kThreads) phase_v (Args<T> a)
   double vals[1] = { (double) e.acc };
   const int ks[1] = { kRhV };
   store_parts<1> (vals, a.part, a.grid, ks);
-  if (!arrive_last (st, a.grid))
-    return;
+}
+
+// alpha from (rh, v), or a breakdown.
+__device__ __forceinline__ void tail_v (DevState *st, const double *part, int grid)
+{
   double sv[1];
-  sum_parts<1> (a.part, a.grid, ks, sv);
+  const int ks[1] = { kRhV };
+  sum_parts<1> (part, grid, ks, sv);
   if (threadIdx.x == 0)
     {
       const double alpha = st->rho / sv[0]; // gpu/bicgstab.cu:466
@@ -399,23 +405,22 @@ __global__ void __launch_bounds__ (kThreads) phase_v (Args<T> a)
     }
 }
 
-// phase 4: t = A z, partials (t, s), (t, t); its last CTA derives omega.
-template <typename T, class Op>
-__global__ void __launch_bounds__ (kThreads) phase_t (Args<T> a)
+// phase 4: t = A z, partials (t, s), (t, t).
+template <typename T, class Op> __device__ __forceinline__ void body_t (const Args<T> &a)
 {
-  DevState *st = a.st;
-  const int2 f = flags (st);
-  if (f.x || f.y)
-    return;
   EpiTS<T> e{ a.s };
   Op::run (a, a.z, a.t, e);
   double vals[2] = { (double) e.ts, (double) e.tt };
   const int ks[2] = { kTS, kTT };
   store_parts<2> (vals, a.part, a.grid, ks);
-  if (!arrive_last (st, a.grid))
-    return;
+}
+
+// omega from (t, s) and (t, t), or a breakdown.
+__device__ __forceinline__ void tail_t (DevState *st, const double *part, int grid)
+{
   double sv[2];
-  sum_parts<2> (a.part, a.grid, ks, sv);
+  const int ks[2] = { kTS, kTT };
+  sum_parts<2> (part, grid, ks, sv);
   if (threadIdx.x == 0)
     {
       const double omega = sv[1] != 0.0 ? sv[0] / sv[1] : 0.0; // :488
@@ -428,6 +433,51 @@ __global__ void __launch_bounds__ (kThreads) phase_t (Args<T> a)
           *reinterpret_cast<volatile int *> (&st->done) = 1;
         }
     }
+}
+
+// End of an iteration: the decision that opens the next one, from (rh, r),
+// (r, r) and (x', x') of phase 5, or in a replacement iteration from r,
+// (rh, r) and (r, r) of phase 2 and (g, g) of phase 1.
+__device__ __forceinline__ void tail_end (DevState *st, const double *part, int grid, bool rep)
+{
+  double sv[3];
+  const int ks[3] = { kRhR, kRR, rep ? kGG : kXX };
+  sum_parts<3> (part, grid, ks, sv);
+  if (threadIdx.x == 0)
+    {
+      if (!rep)
+        {
+          st->rho_prev = st->rho;
+          st->iter = st->iter + 1;
+        }
+      decide (st, sv[0], sv[1], sv[2], rep);
+    }
+}
+
+template <typename T, class Op>
+__global__ void __launch_bounds__ (kThreads) phase_v (Args<T> a)
+{
+  DevState *st = a.st;
+  const int2 f = flags (st);
+  if (f.x)
+    return;
+  body_v<T, Op> (a, st, f.y != 0);
+  if (f.y || !arrive_last (st, a.grid))
+    return;
+  tail_v (st, a.part, a.grid);
+}
+
+template <typename T, class Op>
+__global__ void __launch_bounds__ (kThreads) phase_t (Args<T> a)
+{
+  DevState *st = a.st;
+  const int2 f = flags (st);
+  if (f.x || f.y)
+    return;
+  body_t<T, Op> (a);
+  if (!arrive_last (st, a.grid))
+    return;
+  tail_t (st, a.part, a.grid);
 }
 
 // r = b - A x (x given), partials ||r||^2, ||b||^2 — the true residual.
@@ -550,15 +600,10 @@ __device__ __forceinline__ void block_row_apply (const Args<T> &a, int64_t br, T
 // phase 1: p = r + beta (p - omega v) (q = M^-1 p), with beta from the
 // decision that closed the previous kernel; in a replacement iteration the
 // fold g += x', x' = 0 and the partial (g, g) instead.
-template <typename T, int PK>
-__global__ void __launch_bounds__ (kThreads) phase_p (Args<T> a)
+template <typename T, int PK> __device__ __forceinline__ void body_p (const Args<T> &a, const DevState *sc, bool rep)
 {
-  DevState *st = a.st;
-  const int2 f = flags (st);
-  if (f.x)
-    return;
   const int64_t stride = (int64_t) gridDim.x * blockDim.x;
-  if (f.y)
+  if (rep)
     {
       // Group update: fold the accumulated updates into the base, which
       // phase 2 multiplies by A for the true residual.
@@ -575,7 +620,7 @@ __global__ void __launch_bounds__ (kThreads) phase_p (Args<T> a)
       store_parts<1> (vals, a.part, a.grid, kg);
       return;
     }
-  const T tb = (T) st->beta, tw = (T) st->omega;
+  const T tb = (T) sc->beta, tw = (T) sc->omega;
   if constexpr (PK >= kPreBlock2)
     {
       // block Jacobi: one block row per thread, q = Minv p of the block
@@ -617,15 +662,9 @@ __global__ void __launch_bounds__ (kThreads) phase_p (Args<T> a)
 }
 
 // phase 3
-template <typename T, int PK>
-__global__ void __launch_bounds__ (kThreads) phase_s (Args<T> a)
+template <typename T, int PK> __device__ __forceinline__ void body_s (const Args<T> &a, const DevState *sc)
 {
-  DevState *st = a.st;
-  const int2 f = flags (st);
-  if (f.x || f.y)
-    return;
-  const double alpha = st->alpha; // phase 2's last CTA
-  const T ta = (T) alpha;
+  const T ta = (T) sc->alpha;
   const int64_t stride = (int64_t) gridDim.x * blockDim.x;
   if constexpr (PK >= kPreBlock2)
     {
@@ -665,29 +704,11 @@ __global__ void __launch_bounds__ (kThreads) phase_s (Args<T> a)
 // phase 5: x' += alpha q + omega z, r = s - omega t, partials (rh, r),
 // (r, r), (x', x'); its last CTA takes the decision that opens the next
 // iteration.
-template <typename T, int PK>
-__global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
+template <typename T, int PK> __device__ __forceinline__ void body_x (const Args<T> &a, const DevState *sc)
 {
-  DevState *st = a.st;
-  const int2 f = flags (st);
-  if (f.x)
-    return;
-  if (f.y)
-    {
-      // r, (rh, r) and (r, r) came from phase 2 and (g, g) from phase 1:
-      // the last CTA takes the decision that opens the next iteration.
-      if (!arrive_last (st, a.grid))
-        return;
-      double sv[3];
-      const int ks[3] = { kRhR, kRR, kGG };
-      sum_parts<3> (a.part, a.grid, ks, sv);
-      if (threadIdx.x == 0)
-        decide (st, sv[0], sv[1], sv[2], true);
-      return;
-    }
-  const T ta = (T) st->alpha, tw = (T) st->omega;
+  const T ta = (T) sc->alpha, tw = (T) sc->omega;
   // (x', x') feeds the replacement bound only: skipped (0) when it is off.
-  const bool track = st->eps > 0.0;
+  const bool track = sc->eps > 0.0;
   T rhr = 0, rr = 0, xx = 0;
   const T *qa = PK != kPreNone ? a.q : a.p;
   const T *za = PK != kPreNone ? a.z : a.s;
@@ -736,15 +757,160 @@ __global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
   double vals[3] = { (double) rhr, (double) rr, (double) xx };
   const int kk[3] = { kRhR, kRR, kXX };
   store_parts<3> (vals, a.part, a.grid, kk);
+}
+
+template <typename T, int PK>
+__global__ void __launch_bounds__ (kThreads) phase_p (Args<T> a)
+{
+  const int2 f = flags (a.st);
+  if (f.x)
+    return;
+  body_p<T, PK> (a, a.st, f.y != 0);
+}
+
+template <typename T, int PK>
+__global__ void __launch_bounds__ (kThreads) phase_s (Args<T> a)
+{
+  const int2 f = flags (a.st);
+  if (f.x || f.y)
+    return;
+  body_s<T, PK> (a, a.st);
+}
+
+// phase 5 ends the iteration: its last CTA takes the decision that opens the
+// next one (in a replacement iteration on phase 1 and 2's partials).
+template <typename T, int PK>
+__global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
+{
+  DevState *st = a.st;
+  const int2 f = flags (st);
+  if (f.x)
+    return;
+  if (!f.y)
+    body_x<T, PK> (a, st);
   if (!arrive_last (st, a.grid))
     return;
-  double sv[3];
-  sum_parts<3> (a.part, a.grid, kk, sv);
+  tail_end (st, a.part, a.grid, f.y != 0);
+}
+
+// ------------------------------------------------------------ persistent iteration
+
+// A grid barrier waits at most this long (the longest phase of the largest
+// system this engine runs takes milliseconds); past it the CTA records a
+// fault and leaves, and so does every CTA behind a later barrier.
+constexpr unsigned long long kBarrierLimitNs = 4000000000ull;
+
+// Scalar rows from which the auto launch mode runs the persistent kernel.
+constexpr int64_t kPersistentRows = 1000000;
+
+__device__ __forceinline__ unsigned long long global_ns ()
+{
+  unsigned long long t;
+  asm volatile ("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Barrier over the whole cooperative grid, after which every CTA sees every
+// CTA's writes from before it. Thread 0 of each CTA counts the CTA in with an
+// acq_rel add; the last one in runs `tail` (the phase's scalar work, with the
+// whole CTA, on the device state) before it resets the count and advances
+// the generation with a release; the others wait for that with a bounded
+// acquire poll. gen is thread 0's copy of the generation. False when the wait
+// gave up (the fault is recorded): the caller must return. (Two-level
+// arrival through counters of 4 or 16 CTAs, and polls backing off to 32 or
+// 256 ns, measured slower on GB300: 33-34 against 29 us per iteration at
+// 20 000 rows.)
+template <class Tail> __device__ __forceinline__ bool grid_sync (DevState *st, int grid, unsigned &gen, Tail tail)
+{
+  __shared__ int s_last, s_ok;
+  __syncthreads ();
+  cuda::atomic_ref<unsigned, cuda::thread_scope_device> arrive (st->arrive);
+  cuda::atomic_ref<unsigned, cuda::thread_scope_device> g (st->gen);
   if (threadIdx.x == 0)
     {
-      st->rho_prev = st->rho;
-      st->iter = st->iter + 1;
-      decide (st, sv[0], sv[1], sv[2], false);
+      int ok = 1;
+      const int last = arrive.fetch_add (1u, cuda::memory_order_acq_rel) == (unsigned) grid - 1;
+      if (!last)
+        {
+          const unsigned long long t0 = global_ns ();
+          unsigned polls = 0;
+          while (g.load (cuda::memory_order_acquire) == gen)
+            {
+              if ((++polls & 255u) == 0 && global_ns () - t0 > kBarrierLimitNs)
+                {
+                  ok = 0;
+                  cuda::atomic_ref<int, cuda::thread_scope_device> fault (st->fault);
+                  fault.store (1, cuda::memory_order_relaxed);
+                  break;
+                }
+              __nanosleep (20);
+            }
+        }
+      gen++;
+      s_last = last;
+      s_ok = ok;
+    }
+  __syncthreads ();
+  if (s_last)
+    {
+      tail ();
+      __syncthreads ();
+      if (threadIdx.x == 0)
+        {
+          arrive.store (0u, cuda::memory_order_relaxed);
+          g.store (gen, cuda::memory_order_release);
+        }
+    }
+  return s_ok != 0;
+}
+
+// Up to `iters` BiCGStab iterations in one cooperative launch: the five phase
+// bodies separated by grid barriers instead of kernel boundaries, the scalar
+// work of a phase done by the last CTA to reach its barrier, on the device
+// state, as the last CTA of the phase kernels does it (the same sums in the
+// same order: the same bits). The x vector of each product was written by
+// other CTAs of this kernel, so the products load it coherently (XCoh).
+template <typename T, class Op, int PK>
+__global__ void __launch_bounds__ (kThreads, 4) iterate_kernel (Args<T> a, int iters)
+{
+  DevState *st = a.st;
+  unsigned gen = 0;
+  if (threadIdx.x == 0)
+    gen = cuda::atomic_ref<unsigned, cuda::thread_scope_device> (st->gen).load (cuda::memory_order_relaxed);
+  const double *part = a.part;
+  const int grid = a.grid;
+  auto none = [] () {};
+  for (int it = 0; it < iters; it++)
+    {
+      const int2 f = flags (st);
+      if (f.x)
+        break;
+      const bool rep = f.y != 0;
+      body_p<T, PK> (a, st, rep);
+      if (!grid_sync (st, grid, gen, none))
+        return;
+      body_v<T, Op> (a, st, rep);
+      if (rep)
+        {
+          if (!grid_sync (st, grid, gen, [&] () { tail_end (st, part, grid, true); }))
+            return;
+          continue;
+        }
+      if (!grid_sync (st, grid, gen, [&] () { tail_v (st, part, grid); }))
+        return;
+      if (flags (st).x)
+        break;
+      body_s<T, PK> (a, st);
+      if (!grid_sync (st, grid, gen, none))
+        return;
+      body_t<T, Op> (a);
+      if (!grid_sync (st, grid, gen, [&] () { tail_t (st, part, grid); }))
+        return;
+      if (flags (st).x)
+        break;
+      body_x<T, PK> (a, st);
+      if (!grid_sync (st, grid, gen, [&] () { tail_end (st, part, grid, false); }))
+        return;
     }
 }
 
@@ -899,19 +1065,19 @@ enum SpmvKind
   kTprAny
 };
 
-template <typename T, int K> struct OpOf;
-template <typename T> struct OpOf<T, kCsr8> { using type = CsrOp<T, 8>; };
+template <typename T, int K, class XL = dev::XNc> struct OpOf;
+template <typename T, class XL> struct OpOf<T, kCsr8, XL> { using type = CsrOp<T, 8, XL>; };
 // Few lanes per block row: every lane then holds whole block lines, so the
 // warp-level FP64 instructions are not spent on predicated-off lanes or on
 // shuffle-reduction adds (each FP64 warp instruction costs the same issue
 // time on GB300's narrow FP64 pipe however many lanes are active).
-template <typename T> struct OpOf<T, kFlat2> { using type = FlatOp<T, 2, 2>; };
-template <typename T> struct OpOf<T, kFlat4> { using type = FlatOp<T, 4, 4>; };
-template <typename T> struct OpOf<T, kFlat8> { using type = FlatOp<T, 8, 4>; };
-template <typename T> struct OpOf<T, kFlat16> { using type = FlatOp<T, 16, 8>; };
-template <typename T> struct OpOf<T, kFlat32> { using type = FlatOp<T, 32, 16>; };
-template <typename T> struct OpOf<T, kTpr3> { using type = TprOp<T, 3>; };
-template <typename T> struct OpOf<T, kTprAny> { using type = TprOp<T, 0>; };
+template <typename T, class XL> struct OpOf<T, kFlat2, XL> { using type = FlatOp<T, 2, 2, XL>; };
+template <typename T, class XL> struct OpOf<T, kFlat4, XL> { using type = FlatOp<T, 4, 4, XL>; };
+template <typename T, class XL> struct OpOf<T, kFlat8, XL> { using type = FlatOp<T, 8, 4, XL>; };
+template <typename T, class XL> struct OpOf<T, kFlat16, XL> { using type = FlatOp<T, 16, 8, XL>; };
+template <typename T, class XL> struct OpOf<T, kFlat32, XL> { using type = FlatOp<T, 32, 16, XL>; };
+template <typename T, class XL> struct OpOf<T, kTpr3, XL> { using type = TprOp<T, 3, XL>; };
+template <typename T, class XL> struct OpOf<T, kTprAny, XL> { using type = TprOp<T, 0, XL>; };
 
 int spmv_kind_for (const bmfp_matrix_s *A)
 {
@@ -1020,6 +1186,34 @@ template <typename T> void launch_vector_phase (int pk, int phase, const Args<T>
     }
 }
 
+template <typename T, int K> const void *iterate_for_pre (int pk)
+{
+  using Op = typename OpOf<T, K, dev::XCoh>::type;
+  if (pk == kPreNone)
+    return reinterpret_cast<const void *> (&iterate_kernel<T, Op, kPreNone>);
+  if (pk == kPrePoint)
+    return reinterpret_cast<const void *> (&iterate_kernel<T, Op, kPrePoint>);
+  return nullptr; // block Jacobi runs as graphs
+}
+
+// The persistent iteration kernel for a product kind and preconditioner, or
+// null. Its grid must fit the device at once (4 CTAs of 256 threads per SM,
+// 64 registers a thread): the products of bs 8, 16 and 32 need more
+// registers than that, and with their long rows the launch gaps the kernel
+// saves matter least; they run as graphs.
+template <typename T> const void *iterate_for (int kind, int pk)
+{
+  switch (kind)
+    {
+    case kCsr8: return iterate_for_pre<T, kCsr8> (pk);
+    case kFlat2: return iterate_for_pre<T, kFlat2> (pk);
+    case kFlat4: return iterate_for_pre<T, kFlat4> (pk);
+    case kTpr3: return iterate_for_pre<T, kTpr3> (pk);
+    case kTprAny: return iterate_for_pre<T, kTprAny> (pk);
+    default: return nullptr;
+    }
+}
+
 // Unit roundoff of the engine's precision (replacement bound).
 double unit_roundoff (int dtype) { return dtype == BMFP_R64F ? 0x1p-53 : 0x1p-24; }
 
@@ -1076,7 +1270,8 @@ WideEngine::~WideEngine ()
     cudaFreeHost (h_state_);
 }
 
-int WideEngine::init (const bmfp_matrix_s *A, int precond, int chunk, cudaStream_t stream, int ctas_per_sm)
+int WideEngine::init (const bmfp_matrix_s *A, int precond, int chunk, cudaStream_t stream, int ctas_per_sm,
+                      int launch_mode)
 {
   if (!A)
     return fail (BMFP_ERROR_INVALID_VALUE, "null matrix");
@@ -1132,8 +1327,9 @@ int WideEngine::init (const bmfp_matrix_s *A, int precond, int chunk, cudaStream
       q_ = nullptr;
       z_ = nullptr;
     }
-  BMFP_CUDA (cudaMalloc (&part_, sizeof (double) * (size_t) kParts * grid_));
-  BMFP_CUDA (cudaMemsetAsync (part_, 0, sizeof (double) * (size_t) kParts * grid_, stream));
+    part_bytes_ = sizeof (double) * (size_t) kParts * grid_;
+  BMFP_CUDA (cudaMalloc (&part_, part_bytes_));
+  BMFP_CUDA (cudaMemsetAsync (part_, 0, part_bytes_, stream));
   BMFP_CUDA (cudaMalloc (&state_, sizeof (DevState)));
   BMFP_CUDA (cudaMemsetAsync (state_, 0, sizeof (DevState), stream));
   BMFP_CUDA (cudaMallocHost (&h_state_, 2 * sizeof (DevState)));
@@ -1143,7 +1339,66 @@ int WideEngine::init (const bmfp_matrix_s *A, int precond, int chunk, cudaStream
   int rc = matrix_bound (A, grid_, &cA_, stream); // synchronises the stream
   if (rc != BMFP_SUCCESS)
     return rc;
-  return capture (capture_stream_);
+  // Persistent iterations need a cooperative launch whose CTAs all fit on
+  // the device at once. Auto takes them from kPersistentRows up: their grid
+  // barriers cost more than the graph's kernel boundaries, their phases run
+  // faster, and the second wins on large systems only (Q4 elasticity, FP64,
+  // us per iteration, graph / persistent: 20 000 rows 29.4 / 29.2, 245 000
+  // rows 53.6 / 56.5, 500 000 rows 79.2 / 84.4, 1.1 M rows 148.3 / 142.0,
+  // 2 M rows 250.2 / 233.1).
+  iterate_ = nullptr;
+  if (launch_mode == BMFP_LAUNCH_PERSISTENT || (launch_mode == BMFP_LAUNCH_AUTO && n_ >= kPersistentRows))
+    {
+      const void *fn = dtype_ == BMFP_R64F ? iterate_for<double> (spmv_kind_, pre_kind_)
+                                           : iterate_for<float> (spmv_kind_, pre_kind_);
+      int coop = 0, per_sm = 0;
+      BMFP_CUDA (cudaDeviceGetAttribute (&coop, cudaDevAttrCooperativeLaunch, dev));
+      if (fn && coop)
+        BMFP_CUDA (cudaOccupancyMaxActiveBlocksPerMultiprocessor (&per_sm, fn, kThreads, 0));
+      if (fn && coop && (int64_t) per_sm * sms >= grid_)
+        iterate_ = fn;
+      else if (launch_mode == BMFP_LAUNCH_PERSISTENT)
+        return fail (BMFP_ERROR_NOT_SUPPORTED,
+                     "persistent iterations need no preconditioner or point Jacobi and a grid the "
+                     "device holds at once (%d CTAs, %d per SM fit)",
+                     grid_, per_sm);
+    }
+  return iterate_ ? BMFP_SUCCESS : capture (capture_stream_);
+}
+
+int WideEngine::launch_iterations (cudaStream_t s)
+{
+  void *q = jacobi_ ? q_ : p_;
+  void *z = jacobi_ ? z_ : s_;
+  int iters = chunk_;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3 ((unsigned) grid_);
+  cfg.blockDim = dim3 (kThreads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaError_t e;
+  if (dtype_ == BMFP_R64F)
+    {
+      Args<double> a
+        = make_args<double> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, g_, xp_, part_, grid_, state_);
+      void *args[] = { &a, &iters };
+      e = cudaLaunchKernelExC (&cfg, iterate_, args);
+    }
+  else
+    {
+      Args<float> a
+        = make_args<float> (A_, n_, x_, r_, rh_, p_, v_, q, s_, z, t_, P_, g_, xp_, part_, grid_, state_);
+      void *args[] = { &a, &iters };
+      e = cudaLaunchKernelExC (&cfg, iterate_, args);
+    }
+  if (e != cudaSuccess)
+    return cuda_fail (e, "cooperative launch of the iteration kernel", __FILE__, __LINE__);
+  return BMFP_SUCCESS;
 }
 
 int WideEngine::launch_phase (int phase, cudaStream_t s)
@@ -1252,6 +1507,18 @@ __global__ void stop_kernel (DevState *st)
 }
 } // namespace
 
+// A barrier of the persistent kernel gave up: the barrier words may hold a
+// partial count, so the state (and the partials) are cleared (the next solve
+// starts a new run) and the solve fails.
+int WideEngine::barrier_fault (cudaStream_t s)
+{
+  BMFP_CUDA (cudaStreamSynchronize (s));
+  BMFP_CUDA (cudaMemsetAsync (state_, 0, sizeof (DevState), s));
+  BMFP_CUDA (cudaMemsetAsync (part_, 0, part_bytes_, s));
+  BMFP_CUDA (cudaStreamSynchronize (s));
+  return fail (BMFP_ERROR_TIMEOUT, "a grid barrier of the iteration kernel gave up waiting");
+}
+
 int WideEngine::run (cudaStream_t s, DevState *out, void *d_snap, double *snap_rr, int stall)
 {
   // Keep one graph in flight while the host inspects the previous one.
@@ -1266,13 +1533,22 @@ int WideEngine::run (cudaStream_t s, DevState *out, void *d_snap, double *snap_r
   bool stopping = false;
   for (;; k++)
     {
-      BMFP_CUDA (cudaGraphLaunch (graph_, s));
+      if (iterate_)
+        {
+          const int rc = launch_iterations (s);
+          if (rc != BMFP_SUCCESS)
+            return rc;
+        }
+      else
+        BMFP_CUDA (cudaGraphLaunch (graph_, s));
       BMFP_CUDA (cudaMemcpyAsync (&h_state_[k & 1], state_, sizeof (DevState), cudaMemcpyDeviceToHost, s));
       BMFP_CUDA (cudaEventRecord (ev_[k & 1], s));
       if (k > 0)
         {
           BMFP_CUDA (cudaEventSynchronize (ev_[(k - 1) & 1]));
           const DevState &h = h_state_[(k - 1) & 1];
+          if (h.fault)
+            return barrier_fault (s);
           if (snap_k == k - 1)
             *snap_rr = snap_at = h.rr;
           if (h.done)
@@ -1313,6 +1589,8 @@ int WideEngine::run (cudaStream_t s, DevState *out, void *d_snap, double *snap_r
     }
   BMFP_CUDA (cudaStreamSynchronize (s));
   *out = h_state_[k & 1];
+  if (out->fault)
+    return barrier_fault (s);
   if (snap_k == k && snap_rr)
     *snap_rr = out->rr;
   // The run's result into x: the snapshot when the run ended above the best

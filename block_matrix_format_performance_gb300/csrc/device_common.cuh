@@ -64,6 +64,59 @@ __device__ __forceinline__ void ld_cached2 (const double *p, double &a, double &
 template <typename T> __device__ __forceinline__ T ld_stream (const T *p) { return __ldcs (p); }
 template <typename T> __device__ __forceinline__ T ld_cached (const T *p) { return __ldg (p); }
 
+// How the row routines load the vector they multiply.
+// XNc: the read-only path, for a vector no thread of the running kernel writes.
+struct XNc
+{
+  template <typename T> __device__ static __forceinline__ Vec16<T> ld16 (const T *p) { return ld_cached16 (p); }
+  template <typename T> __device__ static __forceinline__ void ld2 (const T *p, T &a, T &b) { ld_cached2 (p, a, b); }
+  template <typename T> __device__ static __forceinline__ T ld (const T *p) { return __ldg (p); }
+};
+
+// XCoh: plain (weak, L1-cached) global loads, for a vector that other CTAs of
+// the same persistent kernel wrote before a grid barrier. The barrier's
+// release/acquire pair orders those writes before these loads; the
+// read-only path has no such guarantee for data written during the kernel.
+// volatile keeps the compiler from merging or moving the loads across the
+// barrier between two iterations.
+struct XCoh
+{
+  __device__ static __forceinline__ Vec16<double> ld16 (const double *p)
+  {
+    Vec16<double> r;
+    asm volatile ("ld.global.v2.f64 {%0, %1}, [%2];" : "=d"(r.v[0]), "=d"(r.v[1]) : "l"(p));
+    return r;
+  }
+  __device__ static __forceinline__ Vec16<float> ld16 (const float *p)
+  {
+    Vec16<float> r;
+    asm volatile ("ld.global.v4.f32 {%0, %1, %2, %3}, [%4];"
+                  : "=f"(r.v[0]), "=f"(r.v[1]), "=f"(r.v[2]), "=f"(r.v[3])
+                  : "l"(p));
+    return r;
+  }
+  __device__ static __forceinline__ void ld2 (const double *p, double &a, double &b)
+  {
+    asm volatile ("ld.global.v2.f64 {%0, %1}, [%2];" : "=d"(a), "=d"(b) : "l"(p));
+  }
+  __device__ static __forceinline__ void ld2 (const float *p, float &a, float &b)
+  {
+    asm volatile ("ld.global.v2.f32 {%0, %1}, [%2];" : "=f"(a), "=f"(b) : "l"(p));
+  }
+  __device__ static __forceinline__ double ld (const double *p)
+  {
+    double r;
+    asm volatile ("ld.global.f64 %0, [%1];" : "=d"(r) : "l"(p));
+    return r;
+  }
+  __device__ static __forceinline__ float ld (const float *p)
+  {
+    float r;
+    asm volatile ("ld.global.f32 %0, [%1];" : "=f"(r) : "l"(p));
+    return r;
+  }
+};
+
 // Lane mask of the aligned group of G lanes that contains this lane.
 template <int G> __device__ __forceinline__ unsigned group_mask ()
 {

@@ -502,6 +502,9 @@ void wide_main (bmfp_server_s *sv, int lane)
       if (it == sv->wide_solvers.end ())
         {
           bmfp_solver_options o = sv->opts.solver;
+          // Lanes share the GPU with the batched solver and each other: a
+          // persistent kernel would hold every SM while it runs.
+          o.launch_mode = BMFP_LAUNCH_GRAPH;
           rc = bmfp_solver_create (&solver, const_cast<bmfp_matrix_s *> (r->A), &o, stream);
           if (rc == BMFP_SUCCESS)
             sv->wide_solvers[key] = solver;

@@ -55,6 +55,8 @@ struct DevState
   int status;      // 0 running, 1 converged, 2 iteration limit, 3 breakdown
   int replacements;
   unsigned arrive; // CTAs of the running kernel that have written their partials
+  unsigned gen;    // grid barriers passed by the persistent iteration kernel
+  int fault;       // a grid barrier of that kernel gave up waiting
   int pad;
 };
 
@@ -96,7 +98,9 @@ public:
   WideEngine &operator= (const WideEngine &) = delete;
 
   // precond: BMFP_PRECOND_NONE, _JACOBI (point) or _BLOCK_JACOBI (bs <= 8).
-  int init (const bmfp_matrix_s *A, int precond, int chunk, cudaStream_t stream, int ctas_per_sm = 4);
+  // launch_mode: enum bmfp_launch_mode.
+  int init (const bmfp_matrix_s *A, int precond, int chunk, cudaStream_t stream, int ctas_per_sm = 4,
+            int launch_mode = 0);
   // Residual replacement on (default for FP64 engines) or off (the
   // reference's plain recurrences; FP32 engines always run without it).
   void set_replacement (bool on) { replace_ = on && dtype_ == BMFP_R64F; }
@@ -137,6 +141,8 @@ public:
 private:
   int capture (cudaStream_t stream);
   int launch_phase (int phase, cudaStream_t stream);
+  int launch_iterations (cudaStream_t stream);
+  int barrier_fault (cudaStream_t stream);
   int start (bool zero, const void *c, double tol, int max_iter, double norm_b, int iter0, bool new_shadow,
              cudaStream_t s);
 
@@ -156,9 +162,11 @@ private:
   void *q_ = nullptr, *s_ = nullptr, *z_ = nullptr, *t_ = nullptr, *P_ = nullptr;
   void *g_ = nullptr, *xp_ = nullptr;
   double *part_ = nullptr;
+  size_t part_bytes_ = 0;
   DevState *state_ = nullptr;
   DevState *h_state_ = nullptr; // pinned, two slots
   cudaGraphExec_t graph_ = nullptr;
+  const void *iterate_ = nullptr; // persistent iteration kernel, or null: graphs
   cudaStream_t capture_stream_ = nullptr;
   cudaEvent_t ev_[2] = { nullptr, nullptr };
 };

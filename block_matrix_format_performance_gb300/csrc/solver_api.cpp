@@ -363,6 +363,7 @@ void bmfp_solver_options_init (bmfp_solver_options *o)
   o->ctas_per_sm = 4;
   o->inner_stall_iterations = 64;
   o->residual_replacement = 1;
+  o->launch_mode = BMFP_LAUNCH_AUTO;
 }
 
 int bmfp_solver_create (bmfp_solver_t *out, bmfp_matrix_t A, const bmfp_solver_options *opts,
@@ -383,6 +384,8 @@ int bmfp_solver_create (bmfp_solver_t *out, bmfp_matrix_t A, const bmfp_solver_o
   if (!(o.tolerance > 0) || o.max_iterations < 0 || o.iterations_per_graph < 1 || o.ctas_per_sm < 1
       || o.ctas_per_sm > 8 || o.inner_stall_iterations < 0)
     return fail (BMFP_ERROR_INVALID_VALUE, "invalid tolerance or iteration limits");
+  if (o.launch_mode < BMFP_LAUNCH_AUTO || o.launch_mode > BMFP_LAUNCH_PERSISTENT)
+    return fail (BMFP_ERROR_INVALID_VALUE, "invalid launch mode %d", o.launch_mode);
   if (o.precision == BMFP_SOLVE_MIXED && A->dtype != BMFP_R64F)
     return fail (BMFP_ERROR_INVALID_VALUE, "mixed precision needs an FP64 matrix");
   if (o.precision == BMFP_SOLVE_FP64 && A->dtype != BMFP_R64F)
@@ -410,16 +413,16 @@ int bmfp_solver_create (bmfp_solver_t *out, bmfp_matrix_t A, const bmfp_solver_o
   if (o.precision == BMFP_SOLVE_FP32)
     {
       sv->main.reset (new (std::nothrow) WideEngine);
-      rc = sv->main->init (A32, jac, o.iterations_per_graph, s, o.ctas_per_sm);
+      rc = sv->main->init (A32, jac, o.iterations_per_graph, s, o.ctas_per_sm, o.launch_mode);
     }
   else
     {
       sv->main.reset (new (std::nothrow) WideEngine);
-      rc = sv->main->init (A, jac, o.iterations_per_graph, s, o.ctas_per_sm);
+      rc = sv->main->init (A, jac, o.iterations_per_graph, s, o.ctas_per_sm, o.launch_mode);
       if (rc == BMFP_SUCCESS && o.precision == BMFP_SOLVE_MIXED)
         {
           sv->inner.reset (new (std::nothrow) WideEngine);
-          rc = sv->inner->init (A32, jac, o.iterations_per_graph, s, o.ctas_per_sm);
+          rc = sv->inner->init (A32, jac, o.iterations_per_graph, s, o.ctas_per_sm, o.launch_mode);
         }
     }
   if (rc != BMFP_SUCCESS)

@@ -22,7 +22,7 @@ inline constexpr bool flat_block_size (int bs) { return bs == 2 || bs == 4 || bs
 
 // One block row by an aligned group of G lanes, 16-byte vector loads.
 // Requires bs in {2,4,8,16,32}, G*V >= bs and 16-byte aligned vals and x.
-template <typename T, int BS, int G, int U, class Epi>
+template <typename T, int BS, int G, int U, class XL = dev::XNc, class Epi>
 __device__ __forceinline__ void flat_row (int row, const int *__restrict__ row_ptr,
                                           const int *__restrict__ cols, const T *__restrict__ vals,
                                           const T *__restrict__ x, T *__restrict__ y, Epi &epi)
@@ -69,7 +69,7 @@ __device__ __forceinline__ void flat_row (int row, const int *__restrict__ row_p
 #pragma unroll
               for (int u = 0; u < U; u++)
                 {
-                  const V16 xv = dev::ld_cached16 (x + (size_t) c[u] * BS + c0);
+                  const V16 xv = XL::ld16 (x + (size_t) c[u] * BS + c0);
 #pragma unroll
                   for (int v = 0; v < V; v++)
                     acc = fma (a[u].v[v], xv.v[v], acc);
@@ -81,7 +81,7 @@ __device__ __forceinline__ void flat_row (int row, const int *__restrict__ row_p
               if (b < nblk)
                 {
                   const V16 av = dev::ld_stream16 (vb + b * E + o);
-                  const V16 xv = dev::ld_cached16 (x + (size_t) __ldg (cb + b) * BS + c0);
+                  const V16 xv = XL::ld16 (x + (size_t) __ldg (cb + b) * BS + c0);
 #pragma unroll
                   for (int v = 0; v < V; v++)
                     acc = fma (av.v[v], xv.v[v], acc);
@@ -119,7 +119,7 @@ __device__ __forceinline__ void flat_row (int row, const int *__restrict__ row_p
               for (int u = 0; u < U; u++)
                 {
                   T x0, x1;
-                  dev::ld_cached2 (x + (size_t) c[u] * 2, x0, x1);
+                  XL::ld2 (x + (size_t) c[u] * 2, x0, x1);
                   acc0 = fma (a[u].v[0], x0, acc0);
                   acc0 = fma (a[u].v[1], x1, acc0);
                   acc1 = fma (a[u].v[2], x0, acc1);
@@ -133,7 +133,7 @@ __device__ __forceinline__ void flat_row (int row, const int *__restrict__ row_p
                 {
                   const V16 av = dev::ld_stream16 (vb + b * E);
                   T x0, x1;
-                  dev::ld_cached2 (x + (size_t) __ldg (cb + b) * 2, x0, x1);
+                  XL::ld2 (x + (size_t) __ldg (cb + b) * 2, x0, x1);
                   acc0 = fma (av.v[0], x0, acc0);
                   acc0 = fma (av.v[1], x1, acc0);
                   acc1 = fma (av.v[2], x0, acc1);
@@ -171,7 +171,7 @@ __device__ __forceinline__ void flat_row (int row, const int *__restrict__ row_p
           for (int p = 0; p < NP; p++)
             a[p] = dev::ld_stream16 (blk + p * CH);
           const int c = __ldg (cb + b);
-          const V16 xv = dev::ld_cached16 (x + (size_t) c * BS + c0);
+          const V16 xv = XL::ld16 (x + (size_t) c * BS + c0);
 #pragma unroll
           for (int p = 0; p < NP; p++)
 #pragma unroll
@@ -243,7 +243,7 @@ __device__ __forceinline__ void rowown_row (int row, const int *__restrict__ row
 
 // One block row by a whole warp, lane (q, r) = (lane / bs, lane % bs), any
 // bs <= 32; scalar loads (no alignment requirement).
-template <typename T, int BSC, class Epi>
+template <typename T, int BSC, class XL = dev::XNc, class Epi>
 __device__ __forceinline__ void tpr_row (int row, int bs_rt, const int *__restrict__ row_ptr,
                                          const int *__restrict__ cols, const T *__restrict__ vals,
                                          const T *__restrict__ x, T *__restrict__ y, Epi &epi)
@@ -261,7 +261,7 @@ __device__ __forceinline__ void tpr_row (int row, int bs_rt, const int *__restri
         const T *a = vals + (size_t) b * bs * bs + r * bs;
         const T *xb = x + (size_t) __ldg (cols + b) * bs;
         for (int c = 0; c < bs; c++)
-          acc = fma (dev::ld_stream (a + c), dev::ld_cached (xb + c), acc);
+          acc = fma (dev::ld_stream (a + c), XL::ld (xb + c), acc);
       }
   int top = 1;
   while (top < Q)
@@ -281,7 +281,7 @@ __device__ __forceinline__ void tpr_row (int row, int bs_rt, const int *__restri
 }
 
 // One CSR row (bs = 1) by an aligned group of G lanes strided over its entries.
-template <typename T, int G, class Epi>
+template <typename T, int G, class XL = dev::XNc, class Epi>
 __device__ __forceinline__ void csr_row (int row, const int *__restrict__ row_ptr,
                                          const int *__restrict__ cols, const T *__restrict__ vals,
                                          const T *__restrict__ x, T *__restrict__ y, Epi &epi)
@@ -294,11 +294,11 @@ __device__ __forceinline__ void csr_row (int row, const int *__restrict__ row_pt
     {
       const T a0 = dev::ld_stream (vals + e), a1 = dev::ld_stream (vals + e + G);
       const int c0 = __ldg (cols + e), c1 = __ldg (cols + e + G);
-      acc0 = fma (a0, dev::ld_cached (x + c0), acc0);
-      acc1 = fma (a1, dev::ld_cached (x + c1), acc1);
+      acc0 = fma (a0, XL::ld (x + c0), acc0);
+      acc1 = fma (a1, XL::ld (x + c1), acc1);
     }
   if (e < end)
-    acc0 = fma (dev::ld_stream (vals + e), dev::ld_cached (x + __ldg (cols + e)), acc0);
+    acc0 = fma (dev::ld_stream (vals + e), XL::ld (x + __ldg (cols + e)), acc0);
   const T acc = dev::group_sum<G> (acc0 + acc1);
   if (gl == 0)
     {

@@ -53,3 +53,13 @@ def test_reference_arm_loads_no_product_code(orc):
     p = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert p.returncode == 0, p.stderr[-2000:]
     assert json.loads(p.stdout.strip().splitlines()[-1])["impl"] == "reference"
+
+
+def test_committed_traffic_names_the_lane_mapping():
+    """The roofline's DRAM traffic comes from a committed ncu capture of the
+    dominant case; it applies only to the lane mapping that capture ran."""
+    sys.path.insert(0, ROOT)
+    import bench
+    t = bench.committed_traffic("bcsr_native_bs32_f64_lanes65")
+    assert t is not None and 6.0e9 < t < 7.0e9
+    assert bench.committed_traffic("bcsr_native_bs32_f64_lanes64") is None

@@ -370,3 +370,101 @@ def test_breakdown_restart_takes_a_new_shadow_residual(lib, cuda):
     assert info["status"] != bm.ERROR_BREAKDOWN, info
     assert rel < max(1e-10, 2 * floor), (rel, floor, info)
     A.close()
+
+
+def _solve_modes(A, b, precision, **kw):
+    """The same solve with the graph of phase kernels and with the persistent
+    iteration kernel."""
+    out = []
+    for mode in ("graph", "persistent"):
+        s = bm.Solver(A, precision, launch_mode=mode, **kw)
+        out.append(s.solve_host(b))
+        s.close()
+    return out
+
+
+def _same_bits(a, b):
+    return a.dtype == b.dtype and np.array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+@pytest.mark.parametrize("case", ["q4", "q4_jacobi", "q4_cps1", "q4_cps2", "csr", "bs3", "bs5", "fp32",
+                                  "mixed", "tiny"])
+def test_persistent_iterations_give_the_graphs_bits(lib, cuda, case):
+    """The persistent kernel runs the phase bodies between grid barriers and
+    derives the scalars in every CTA from the same partials, in the same
+    order, as the phase kernels' last CTA: the same bits, iterations,
+    replacements and restarts, for every product kind it serves."""
+    kw = {}
+    precision = "fp64"
+    if case.startswith("q4"):
+        rp, c, v, b = bm.gen_q4_elasticity(100, 25)
+        A = bm.Matrix.from_bcsr(rp, c, v, 2)
+        if case == "q4_jacobi":
+            kw["preconditioner"] = "jacobi"
+        if case == "q4_cps1":
+            kw["ctas_per_sm"] = 1
+        if case == "q4_cps2":
+            kw["ctas_per_sm"] = 2
+    elif case == "csr":
+        rp, c, v, b = bm.gen_q4_elasticity(30, 8)
+        crp, cc, cv = bm.bcsr_to_csr(rp, c, v, 2)
+        A = bm.Matrix.from_csr(crp, cc, cv, len(crp) - 1)
+        kw["preconditioner"] = "jacobi"
+    elif case in ("bs3", "bs5"):
+        bs = int(case[2])
+        rp, c, v = diag_dominant_bcsr(400, bs, seed=bs)
+        b = np.random.default_rng(3).uniform(-1, 1, 400 * bs)
+        A = bm.Matrix.from_bcsr(rp, c, v, bs)
+    elif case == "fp32":
+        rp, c, v = diag_dominant_bcsr(500, 2, seed=9)
+        b = np.random.default_rng(2).uniform(-1, 1, 1000).astype(np.float32)
+        A = bm.Matrix.from_bcsr(rp, c, v.astype(np.float32), 2)
+        precision = "fp32"
+        kw["tol"] = 1e-5
+    elif case == "mixed":
+        rp, c, v = diag_dominant_bcsr(500, 2, seed=9)
+        b = np.random.default_rng(2).uniform(-1, 1, 1000)
+        A = bm.Matrix.from_bcsr(rp, c, v, 2)
+        precision = "mixed"
+    else:  # a system smaller than one CTA: a grid of one
+        rp, c, v = diag_dominant_bcsr(60, 2, seed=5)
+        b = np.random.default_rng(4).uniform(-1, 1, 120)
+        A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    (xg, ig), (xp, ip) = _solve_modes(A, b, precision, **kw)
+    assert ip["status"] == bm.SUCCESS, ip
+    for k in ("status", "iterations", "iterations_fp32", "refinements", "restarts", "replacements"):
+        assert ig[k] == ip[k], (k, ig, ip)
+    assert _same_bits(xg, xp)
+    if case == "q4":
+        assert ip["replacements"] >= 1  # the replacement iterations ran in the kernel too
+    if case == "mixed":
+        assert ip["iterations_fp32"] > 0  # and the FP32 engine's kernel
+    A.close()
+
+
+def test_persistent_launch_limits(lib, cuda):
+    """Block Jacobi, and a grid the device cannot hold at once (8 CTAs per SM
+    for a system of 160 000 rows: 625 CTAs, 4 per SM fit), run as graphs
+    under auto and are refused when the persistent kernel is asked for."""
+    rp, c, v, b = bm.gen_q4_elasticity(24, 6)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    with pytest.raises(bm.BmfpError) as e:
+        bm.Solver(A, "fp64", launch_mode="persistent", preconditioner="block_jacobi")
+    assert e.value.status == bm.ERROR_NOT_SUPPORTED
+    x, info = bm.Solver(A, "fp64", preconditioner="block_jacobi").solve_host(b)
+    assert info["status"] == bm.SUCCESS
+    rpl, cl, vl, _ = bm.gen_q4_elasticity(400, 200)
+    AL = bm.Matrix.from_bcsr(rpl, cl, vl, 2)
+    with pytest.raises(bm.BmfpError) as e:
+        bm.Solver(AL, "fp64", launch_mode="persistent", ctas_per_sm=8)
+    assert e.value.status == bm.ERROR_NOT_SUPPORTED
+    bm.Solver(AL, "fp64", ctas_per_sm=8).close()
+    bm.Solver(AL, "fp64", launch_mode="persistent", ctas_per_sm=4).close()
+    with pytest.raises(bm.BmfpError) as e:
+        bm.Solver(A, "fp64", launch_mode=3)
+    assert e.value.status == bm.ERROR_INVALID_VALUE
+    rp8, c8, v8 = diag_dominant_bcsr(50, 8, seed=8)
+    A8 = bm.Matrix.from_bcsr(rp8, c8, v8, 8)
+    with pytest.raises(bm.BmfpError) as e:
+        bm.Solver(A8, "fp64", launch_mode="persistent")
+    assert e.value.status == bm.ERROR_NOT_SUPPORTED
