@@ -933,7 +933,8 @@ def fem_small(flush, stream):
 
 def iteration_roofline(grid, hbm_gbs, fp64_gflops, iters=300):
     """Live cost of one FP64 BiCGStab iteration of the whole-GPU engine on
-    the Q4 operator, against its two floors: HBM bytes (2 SpMV + 17 n vector
+    the Q4 operator (the auto launch mode's, with the graph of phase kernels
+    and the persistent kernel beside it), against its two floors: HBM bytes (2 SpMV + 17 n vector
     elements of 8 bytes) over the measured copy bandwidth, and FP64 FMAs
     (8 per block for the two bs-2 products, 12 per row for the epilogue dots
     and vector updates) over the measured FP64 rate. Times `iters`
@@ -945,20 +946,24 @@ def iteration_roofline(grid, hbm_gbs, fp64_gflops, iters=300):
     rp, c, v, rhs = bm.gen_q4_elasticity(nx, ny)
     A = bm.Matrix.from_bcsr(rp, c, v, 2)
     n, nnzb = 2 * nx * ny, int(c.size)
-    sv = bm.Solver(A, "fp64", tol=1e-30, max_iters=iters)
     d_b = torch.from_numpy(rhs).cuda()
     d_x = torch.empty_like(d_b)
-    sv.solve(d_b, d_x)
-    info = min((sv.solve(d_b, d_x) for _ in range(2)), key=lambda i: i["seconds"])
-    sv.close()
+    per_mode = {}
+    for mode in ("graph", "persistent", "auto"):
+        sv = bm.Solver(A, "fp64", tol=1e-30, max_iters=iters, launch_mode=mode)
+        sv.solve(d_b, d_x)
+        info = min((sv.solve(d_b, d_x) for _ in range(2)), key=lambda i: i["seconds"])
+        sv.close()
+        per_mode[mode] = info["seconds"] / max(info["iterations"], 1) * 1e6
     A.close()
-    us = info["seconds"] / max(info["iterations"], 1) * 1e6
+    us = per_mode["auto"]
     nbytes = 2 * bm.bcsr_spmv_bytes(np.float64, nx * ny, nx * ny, 2, nnzb) + 17 * n * 8
     fmas = 8 * nnzb + 12 * n
     hbm_us = nbytes / (hbm_gbs * 1e9) * 1e6
     fp64_us = 2 * fmas / (fp64_gflops * 1e9) * 1e6
     floor = max(hbm_us, fp64_us)
     return {"grid": [nx, ny], "dofs": n, "iterations_timed": info["iterations"], "us_per_iteration": round(us, 2),
+            "graph_us": round(per_mode["graph"], 2), "persistent_us": round(per_mode["persistent"], 2),
             "bytes_per_iteration": int(nbytes), "fp64_fmas_per_iteration": int(fmas),
             "hbm_floor_us": round(hbm_us, 2), "fp64_floor_us": round(fp64_us, 2),
             "floor_us": round(floor, 2), "of_floor": round(floor / us, 3)}

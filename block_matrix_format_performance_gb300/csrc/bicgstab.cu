@@ -800,8 +800,10 @@ __global__ void __launch_bounds__ (kThreads) phase_x (Args<T> a)
 // fault and leaves, and so does every CTA behind a later barrier.
 constexpr unsigned long long kBarrierLimitNs = 4000000000ull;
 
-// Scalar rows from which the auto launch mode runs the persistent kernel.
+// Scalar rows from which the auto launch mode runs the persistent kernel,
+// and its CTAs per SM at most (launch bounds: up to 80 registers a thread).
 constexpr int64_t kPersistentRows = 1000000;
+constexpr int kIterateCtasPerSm = 3;
 
 __device__ __forceinline__ unsigned long long global_ns ()
 {
@@ -871,7 +873,7 @@ template <class Tail> __device__ __forceinline__ bool grid_sync (DevState *st, i
 // same order: the same bits). The x vector of each product was written by
 // other CTAs of this kernel, so the products load it coherently (XCoh).
 template <typename T, class Op, int PK>
-__global__ void __launch_bounds__ (kThreads, 4) iterate_kernel (Args<T> a, int iters)
+__global__ void __launch_bounds__ (kThreads, kIterateCtasPerSm) iterate_kernel (Args<T> a, int iters)
 {
   DevState *st = a.st;
   unsigned gen = 0;
@@ -940,6 +942,10 @@ __global__ void row_norm_kernel (int nbr, int bs, const int *rp, const T *vals, 
                                  int *max_count)
 {
   const int b = bs > 0 ? bs : 1;
+  // Each thread keeps its own maxima, then the warp combines them: one
+  // atomic per warp, not one per row on two addresses.
+  unsigned long long amax = 0;
+  int cmax = 0;
   GRID_STRIDE (i, (int64_t) nbr * b)
   {
     const int br = (int) (i / b), r = (int) (i % b);
@@ -954,9 +960,20 @@ __global__ void row_norm_kernel (int nbr, int bs, const int *rp, const T *vals, 
           sum += fabs ((double) vals[k]);
         count += b;
       }
-    atomicMax (max_abs, (unsigned long long) __double_as_longlong (sum));
-    atomicMax (max_count, count);
+    amax = max (amax, (unsigned long long) __double_as_longlong (sum));
+    cmax = max (cmax, count);
   }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+    {
+      amax = max (amax, __shfl_xor_sync (0xffffffffu, amax, off));
+      cmax = max (cmax, __shfl_xor_sync (0xffffffffu, cmax, off));
+    }
+  if ((threadIdx.x & 31) == 0)
+    {
+      atomicMax (max_abs, amax);
+      atomicMax (max_count, cmax);
+    }
 }
 
 // Point Jacobi from the diagonal blocks: P = 1/a_rr (1 when |a_rr| < 1e-20
@@ -1197,8 +1214,8 @@ template <typename T, int K> const void *iterate_for_pre (int pk)
 }
 
 // The persistent iteration kernel for a product kind and preconditioner, or
-// null. Its grid must fit the device at once (4 CTAs of 256 threads per SM,
-// 64 registers a thread): the products of bs 8, 16 and 32 need more
+// null. Its grid must fit the device at once (3 CTAs of 256 threads per SM,
+// 80 registers a thread): the products of bs 8, 16 and 32 need more
 // registers than that, and with their long rows the launch gaps the kernel
 // saves matter least; they run as graphs.
 template <typename T> const void *iterate_for (int kind, int pk)
@@ -1295,9 +1312,36 @@ int WideEngine::init (const bmfp_matrix_s *A, int precond, int chunk, cudaStream
   int dev = 0, sms = 0;
   BMFP_CUDA (cudaGetDevice (&dev));
   BMFP_CUDA (cudaDeviceGetAttribute (&sms, cudaDevAttrMultiProcessorCount, dev));
-  // Persistent grid: a few CTAs per SM, never more than the rows need.
+  // Persistent iterations need a cooperative launch whose CTAs all fit on
+  // the device at once: at most kIterateCtasPerSm CTAs per SM (the kernel's
+  // launch bounds). Auto takes them from kPersistentRows up (measured on the
+  // Q4 elasticity operator, FP64, us per iteration, graph at 4 CTAs per SM /
+  // persistent at 3: 500 000 rows 79.3 / 79.9, 1.1 M rows 147.7 / 134.3,
+  // 2 M rows 251.3 / 234.0; at 4 CTAs per SM and 64 registers the
+  // persistent kernel spilled and took 84.2 / 142.2 / 234.0).
+  iterate_ = nullptr;
+  int cps = std::max (1, std::min (ctas_per_sm, 8));
+  if (launch_mode == BMFP_LAUNCH_PERSISTENT || (launch_mode == BMFP_LAUNCH_AUTO && n_ >= kPersistentRows))
+    {
+      const void *fn = dtype_ == BMFP_R64F ? iterate_for<double> (spmv_kind_, pre_kind_)
+                                           : iterate_for<float> (spmv_kind_, pre_kind_);
+      int coop = 0, per_sm = 0;
+      BMFP_CUDA (cudaDeviceGetAttribute (&coop, cudaDevAttrCooperativeLaunch, dev));
+      if (fn && coop)
+        BMFP_CUDA (cudaOccupancyMaxActiveBlocksPerMultiprocessor (&per_sm, fn, kThreads, 0));
+      if (fn && coop && per_sm >= 1)
+        {
+          iterate_ = fn;
+          cps = std::min (cps, per_sm);
+        }
+      else if (launch_mode == BMFP_LAUNCH_PERSISTENT)
+        return fail (BMFP_ERROR_NOT_SUPPORTED,
+                     "persistent iterations need no preconditioner or point Jacobi, bs other than 8, 16 "
+                     "and 32, and a device with cooperative launch");
+    }
+  // A few CTAs per SM, never more than the rows need.
   const int64_t want = std::max<int64_t> (1, (n_ + kThreads - 1) / kThreads);
-  grid_ = (int) std::min<int64_t> ((int64_t) sms * std::max (1, std::min (ctas_per_sm, 8)), want);
+  grid_ = (int) std::min<int64_t> ((int64_t) sms * cps, want);
   const size_t S = dtype_size (dtype_);
   const size_t vb = S * (size_t) std::max<int64_t> (n_, 1);
   for (void **ptr : { &x_, &r_, &rh_, &p_, &v_, &s_, &t_, &g_, &xp_ })
@@ -1327,7 +1371,7 @@ int WideEngine::init (const bmfp_matrix_s *A, int precond, int chunk, cudaStream
       q_ = nullptr;
       z_ = nullptr;
     }
-    part_bytes_ = sizeof (double) * (size_t) kParts * grid_;
+  part_bytes_ = sizeof (double) * (size_t) kParts * grid_;
   BMFP_CUDA (cudaMalloc (&part_, part_bytes_));
   BMFP_CUDA (cudaMemsetAsync (part_, 0, part_bytes_, stream));
   BMFP_CUDA (cudaMalloc (&state_, sizeof (DevState)));
@@ -1339,30 +1383,6 @@ int WideEngine::init (const bmfp_matrix_s *A, int precond, int chunk, cudaStream
   int rc = matrix_bound (A, grid_, &cA_, stream); // synchronises the stream
   if (rc != BMFP_SUCCESS)
     return rc;
-  // Persistent iterations need a cooperative launch whose CTAs all fit on
-  // the device at once. Auto takes them from kPersistentRows up: their grid
-  // barriers cost more than the graph's kernel boundaries, their phases run
-  // faster, and the second wins on large systems only (Q4 elasticity, FP64,
-  // us per iteration, graph / persistent: 20 000 rows 29.4 / 29.2, 245 000
-  // rows 53.6 / 56.5, 500 000 rows 79.2 / 84.4, 1.1 M rows 148.3 / 142.0,
-  // 2 M rows 250.2 / 233.1).
-  iterate_ = nullptr;
-  if (launch_mode == BMFP_LAUNCH_PERSISTENT || (launch_mode == BMFP_LAUNCH_AUTO && n_ >= kPersistentRows))
-    {
-      const void *fn = dtype_ == BMFP_R64F ? iterate_for<double> (spmv_kind_, pre_kind_)
-                                           : iterate_for<float> (spmv_kind_, pre_kind_);
-      int coop = 0, per_sm = 0;
-      BMFP_CUDA (cudaDeviceGetAttribute (&coop, cudaDevAttrCooperativeLaunch, dev));
-      if (fn && coop)
-        BMFP_CUDA (cudaOccupancyMaxActiveBlocksPerMultiprocessor (&per_sm, fn, kThreads, 0));
-      if (fn && coop && (int64_t) per_sm * sms >= grid_)
-        iterate_ = fn;
-      else if (launch_mode == BMFP_LAUNCH_PERSISTENT)
-        return fail (BMFP_ERROR_NOT_SUPPORTED,
-                     "persistent iterations need no preconditioner or point Jacobi and a grid the "
-                     "device holds at once (%d CTAs, %d per SM fit)",
-                     grid_, per_sm);
-    }
   return iterate_ ? BMFP_SUCCESS : capture (capture_stream_);
 }
 

@@ -282,9 +282,9 @@ enum bmfp_launch_mode
   BMFP_LAUNCH_AUTO = 0,       /* persistent from 1 000 000 rows up when it can run, else graphs */
   BMFP_LAUNCH_GRAPH = 1,      /* a CUDA graph of five phase kernels per iteration */
   BMFP_LAUNCH_PERSISTENT = 2  /* one cooperative kernel per iterations_per_graph iterations, the
-                                 phases separated by grid barriers (no preconditioner or point
-                                 Jacobi; bs 1-4 or any bs but 8, 16, 32; ctas_per_sm <= 4);
-                                 BMFP_ERROR_NOT_SUPPORTED where it cannot run */
+                                 phases separated by grid barriers, over min(ctas_per_sm, 3) CTAs
+                                 per SM (no preconditioner or point Jacobi; any bs but 8, 16,
+                                 32); BMFP_ERROR_NOT_SUPPORTED where it cannot run */
 };
 
 typedef struct bmfp_solver_options
@@ -315,10 +315,11 @@ typedef struct bmfp_solver_options
                                group update), so stopping on it also meets the tolerance in
                                b - A x; applies when check_true_residual is 1 (with 0 the
                                reference's plain recurrences run) */
-  int launch_mode;          /* enum bmfp_launch_mode (default AUTO). Both modes give the same
-                               bits. The persistent kernel holds every SM for its launch, so
-                               other work on the GPU waits for it (the server's lanes, which
-                               share the GPU with the batched solver, use graphs) */
+  int launch_mode;          /* enum bmfp_launch_mode (default AUTO). On the same grid (ctas_per_sm
+                               <= 3) both modes give the same bits. The persistent kernel holds
+                               every SM for its launch, so other work on the GPU waits for it
+                               (the server's lanes, which share the GPU with the batched
+                               solver, use graphs) */
 } bmfp_solver_options;
 
 typedef struct bmfp_solve_info

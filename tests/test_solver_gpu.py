@@ -394,7 +394,7 @@ def test_persistent_iterations_give_the_graphs_bits(lib, cuda, case):
     derives the scalars in every CTA from the same partials, in the same
     order, as the phase kernels' last CTA: the same bits, iterations,
     replacements and restarts, for every product kind it serves."""
-    kw = {}
+    kw = {"ctas_per_sm": 3}  # the persistent kernel's most; the graph then runs the same grid
     precision = "fp64"
     if case.startswith("q4"):
         rp, c, v, b = bm.gen_q4_elasticity(100, 25)
@@ -443,9 +443,10 @@ def test_persistent_iterations_give_the_graphs_bits(lib, cuda, case):
 
 
 def test_persistent_launch_limits(lib, cuda):
-    """Block Jacobi, and a grid the device cannot hold at once (8 CTAs per SM
-    for a system of 160 000 rows: 625 CTAs, 4 per SM fit), run as graphs
-    under auto and are refused when the persistent kernel is asked for."""
+    """Block Jacobi runs as graphs under auto and is refused when the
+    persistent kernel is asked for. The persistent kernel runs at most 3
+    CTAs per SM: asked for 8 on a system of 160 000 rows (625 CTAs) it runs
+    the grid of 3, and gives the graph's bits at 3."""
     rp, c, v, b = bm.gen_q4_elasticity(24, 6)
     A = bm.Matrix.from_bcsr(rp, c, v, 2)
     with pytest.raises(bm.BmfpError) as e:
@@ -453,13 +454,12 @@ def test_persistent_launch_limits(lib, cuda):
     assert e.value.status == bm.ERROR_NOT_SUPPORTED
     x, info = bm.Solver(A, "fp64", preconditioner="block_jacobi").solve_host(b)
     assert info["status"] == bm.SUCCESS
-    rpl, cl, vl, _ = bm.gen_q4_elasticity(400, 200)
+    rpl, cl, vl, bl = bm.gen_q4_elasticity(400, 200)
     AL = bm.Matrix.from_bcsr(rpl, cl, vl, 2)
-    with pytest.raises(bm.BmfpError) as e:
-        bm.Solver(AL, "fp64", launch_mode="persistent", ctas_per_sm=8)
-    assert e.value.status == bm.ERROR_NOT_SUPPORTED
-    bm.Solver(AL, "fp64", ctas_per_sm=8).close()
-    bm.Solver(AL, "fp64", launch_mode="persistent", ctas_per_sm=4).close()
+    xp, ip = bm.Solver(AL, "fp64", launch_mode="persistent", ctas_per_sm=8, max_iters=200).solve_host(bl)
+    xg, ig = bm.Solver(AL, "fp64", launch_mode="graph", ctas_per_sm=3, max_iters=200).solve_host(bl)
+    assert ip["iterations"] == ig["iterations"] == 200
+    assert _same_bits(xp, xg)
     with pytest.raises(bm.BmfpError) as e:
         bm.Solver(A, "fp64", launch_mode=3)
     assert e.value.status == bm.ERROR_INVALID_VALUE
