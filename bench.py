@@ -812,7 +812,7 @@ def measure_batch(precisions, tol, max_iters, repeats, n_systems=256, per_reques
     for prec in precisions:
         batch = bm.Batch(mats, prec, tol=tol, max_iters=max_iters)
         t0 = time.perf_counter()
-        cluster, threads = batch.autotune(d_b, d_x, probe_iterations=128)
+        cluster, threads = batch.autotune(d_b, d_x, probe_iterations=1024)
         tune_s = time.perf_counter() - t0
         batch.solve(d_b, d_x)
         times, infos = [], None

@@ -76,16 +76,27 @@ __device__ void team_sum (cg::cluster_group &cl, double (&v)[NK], double (&out)[
         sh_cta[k] = a;
       }
   cl.sync ();
-  const unsigned size = cl.num_blocks ();
-#pragma unroll
-  for (int k = 0; k < NK; k++)
+  // Thread 0 adds the CTAs' totals in rank order; the second cluster barrier
+  // publishes the sum to the CTA and keeps sh_cta alive until every CTA has
+  // read it. (Every thread summing the ranks itself issued size warp-wide
+  // FP64 adds per warp and value on GB300's narrow FP64 pipe.)
+  __shared__ double sh_sum[NK];
+  if (threadIdx.x == 0)
     {
-      double a = 0.0;
-      for (unsigned r = 0; r < size; r++)
-        a += *cl.map_shared_rank (&sh_cta[k], r);
-      out[k] = a;
+      const unsigned size = cl.num_blocks ();
+#pragma unroll
+      for (int k = 0; k < NK; k++)
+        {
+          double a = 0.0;
+          for (unsigned r = 0; r < size; r++)
+            a += *cl.map_shared_rank (&sh_cta[k], r);
+          sh_sum[k] = a;
+        }
     }
   cl.sync ();
+#pragma unroll
+  for (int k = 0; k < NK; k++)
+    out[k] = sh_sum[k];
 }
 
 // Team-wide maxima of NK non-negative values.
@@ -116,16 +127,23 @@ __device__ void team_max (cg::cluster_group &cl, double (&v)[NK], double (&out)[
         sh_cta[k] = a;
       }
   cl.sync ();
-  const unsigned size = cl.num_blocks ();
-#pragma unroll
-  for (int k = 0; k < NK; k++)
+  __shared__ double sh_max[NK];
+  if (threadIdx.x == 0)
     {
-      double a = 0.0;
-      for (unsigned r = 0; r < size; r++)
-        a = fmax (a, *cl.map_shared_rank (&sh_cta[k], r));
-      out[k] = a;
+      const unsigned size = cl.num_blocks ();
+#pragma unroll
+      for (int k = 0; k < NK; k++)
+        {
+          double a = 0.0;
+          for (unsigned r = 0; r < size; r++)
+            a = fmax (a, *cl.map_shared_rank (&sh_cta[k], r));
+          sh_max[k] = a;
+        }
     }
   cl.sync ();
+#pragma unroll
+  for (int k = 0; k < NK; k++)
+    out[k] = sh_max[k];
 }
 
 template <typename T> struct TeamSys
@@ -1094,12 +1112,13 @@ int BatchEngine::solve (const void *const *d_b, void *const *d_x, bmfp_solve_inf
 int BatchEngine::autotune (const void *const *d_b, void *const *d_x, cudaStream_t s, int probe_iterations)
 {
   // Time each (cluster, threads) candidate on the real batch with every
-  // system capped at probe_iterations, keep the fastest. A team of one CTA
-  // is never the fastest on these batches (its largest systems take the
-  // longest); a cap of a few iterations times the start of every system
-  // rather than the solves: callers pass a cap near the small systems'
-  // iteration counts (the bench: 128).
-  static const int clusters[] = { 2, 4, 8 };
+  // system capped at probe_iterations, keep the fastest. Teams of 1 or 2
+  // CTAs are never the fastest on these batches (their largest systems take
+  // the longest). The cap decides what is timed: on the uneven elasticity
+  // batch caps of 128-256 iterations time the small systems and pick
+  // 8 x 256 (0.88 s for the full solve), caps of 512 (FP64) or 1024 (mixed)
+  // and more pick 8 x 512 (0.63 s), as the full solves rank them.
+  static const int clusters[] = { 4, 8 };
   static const int threads[] = { 256, 512 };
   int rc = set_vectors (d_b, d_x, s);
   if (rc != BMFP_SUCCESS)

@@ -378,12 +378,14 @@ BMFP_API int bmfp_batch_create (bmfp_batch_t *out, int n_systems, const bmfp_mat
                                 const bmfp_solver_options *opts, void *stream);
 /* Cluster size (1, 2, 4, 8) and threads per CTA (multiple of 64, <= 512). */
 BMFP_API int bmfp_batch_configure (bmfp_batch_t b, int cluster_size, int threads_per_cta);
-/* The project's autotuner: times every (cluster 2, 4, 8) x (threads 256,
- * 512) candidate on this batch with each system capped at probe_iterations
- * and keeps the fastest (a cap near the small systems' iteration counts,
- * e.g. 128, ranks the candidates as the full solve does; a cap of a few
- * iterations times only the systems' starts). Outputs may be NULL.
- * Synchronises the stream. A new batch starts at cluster 8 x 512 threads. */
+/* The project's autotuner: times every (cluster 4, 8) x (threads 256, 512)
+ * candidate on this batch with each system capped at probe_iterations and
+ * keeps the fastest. The cap decides what is timed: it must reach a good
+ * part of the largest systems' iteration counts to rank the candidates as
+ * the full solve does (on the uneven elasticity batch 1024; 128 picks a
+ * configuration 40 % slower), at about 1.3 s per 256 iterations there.
+ * Outputs may be NULL. Synchronises the stream. A new batch starts at
+ * cluster 8 x 512 threads, the fastest on that batch. */
 BMFP_API int bmfp_batch_autotune (bmfp_batch_t b, const void *const *d_b, void *const *d_x,
                                   int probe_iterations, int *cluster_size, int *threads_per_cta,
                                   void *stream);
