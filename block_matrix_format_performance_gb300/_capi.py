@@ -75,6 +75,7 @@ SIGNATURES = {
     "bmfp_solver_create": (c_int, [P(c_void_p), c_void_p, c_void_p, c_void_p]),
     "bmfp_solver_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "bmfp_solver_destroy": (c_int, [c_void_p]),
+    "bmfp_selftest_barrier_timeout": (c_int, [c_double, P(c_int), P(c_double), c_void_p]),
     "bmfp_batch_create": (c_int, [P(c_void_p), c_int, c_void_p, c_void_p, c_void_p]),
     "bmfp_batch_configure": (c_int, [c_void_p, c_int, c_int]),
     "bmfp_batch_autotune": (c_int, [c_void_p, c_void_p, c_void_p, c_int, P(c_int), P(c_int), c_void_p]),

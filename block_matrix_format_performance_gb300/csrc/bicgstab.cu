@@ -822,7 +822,9 @@ __device__ __forceinline__ unsigned long long global_ns ()
 // arrival through counters of 4 or 16 CTAs, and polls backing off to 32 or
 // 256 ns, measured slower on GB300: 33-34 against 29 us per iteration at
 // 20 000 rows.)
-template <class Tail> __device__ __forceinline__ bool grid_sync (DevState *st, int grid, unsigned &gen, Tail tail)
+template <class Tail>
+__device__ __forceinline__ bool grid_sync (DevState *st, int grid, unsigned &gen, Tail tail,
+                                          unsigned long long limit_ns = kBarrierLimitNs)
 {
   __shared__ int s_last, s_ok;
   __syncthreads ();
@@ -838,7 +840,7 @@ template <class Tail> __device__ __forceinline__ bool grid_sync (DevState *st, i
           unsigned polls = 0;
           while (g.load (cuda::memory_order_acquire) == gen)
             {
-              if ((++polls & 255u) == 0 && global_ns () - t0 > kBarrierLimitNs)
+              if ((++polls & 255u) == 0 && global_ns () - t0 > limit_ns)
                 {
                   ok = 0;
                   cuda::atomic_ref<int, cuda::thread_scope_device> fault (st->fault);
@@ -914,6 +916,17 @@ __global__ void __launch_bounds__ (kThreads, kIterateCtasPerSm) iterate_kernel (
       if (!grid_sync (st, grid, gen, [&] () { tail_end (st, part, grid, false); }))
         return;
     }
+}
+
+// The grid barrier's bounded wait, exercised: every CTA waits for one CTA
+// more than the grid holds, so no CTA is ever last; each gives up after
+// limit_ns, records the fault and returns, and the context stays usable.
+__global__ void barrier_selftest_kernel (DevState *st, unsigned long long limit_ns)
+{
+  unsigned gen = 0;
+  if (threadIdx.x == 0)
+    gen = cuda::atomic_ref<unsigned, cuda::thread_scope_device> (st->gen).load (cuda::memory_order_relaxed);
+  grid_sync (st, (int) gridDim.x + 1, gen, [] () {}, limit_ns);
 }
 
 // End of a run: x = e (a fresh solve) or x += e (a restart), with e the run's
@@ -1666,6 +1679,65 @@ int WideEngine::true_residual (const void *d_b, void *d_r, double *rr, double *b
 // allocates nothing (noalloc.cu). They run the same phase kernels as
 // WideEngine, without graphs, and without residual replacement (the
 // reference's plain recurrences).
+
+int barrier_selftest (double limit_s, int *fault, double *elapsed_s, cudaStream_t s)
+{
+  if (!(limit_s > 0.0 && limit_s <= 1.0))
+    return fail (BMFP_ERROR_INVALID_VALUE, "the self-test waits between 0 and 1 s (got %g)", limit_s);
+  int dev = 0, sms = 0, coop = 0;
+  BMFP_CUDA (cudaGetDevice (&dev));
+  BMFP_CUDA (cudaDeviceGetAttribute (&sms, cudaDevAttrMultiProcessorCount, dev));
+  BMFP_CUDA (cudaDeviceGetAttribute (&coop, cudaDevAttrCooperativeLaunch, dev));
+  if (!coop)
+    return fail (BMFP_ERROR_NOT_SUPPORTED, "no cooperative launch on this device");
+  DevState *st = nullptr;
+  BMFP_CUDA (cudaMalloc (&st, sizeof (DevState)));
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaError_t e = cudaMemsetAsync (st, 0, sizeof (DevState), s);
+  if (e == cudaSuccess)
+    e = cudaEventCreate (&a);
+  if (e == cudaSuccess)
+    e = cudaEventCreate (&b);
+  if (e == cudaSuccess)
+    e = cudaEventRecord (a, s);
+  if (e == cudaSuccess)
+    {
+      unsigned long long limit_ns = (unsigned long long) (limit_s * 1e9);
+      void *args[] = { &st, &limit_ns };
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3 ((unsigned) sms);
+      cfg.blockDim = dim3 (kThreads);
+      cfg.stream = s;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeCooperative;
+      attr[0].val.cooperative = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      e = cudaLaunchKernelExC (&cfg, (const void *) barrier_selftest_kernel, args);
+    }
+  DevState h{};
+  if (e == cudaSuccess)
+    e = cudaEventRecord (b, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync (&h, st, sizeof (DevState), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess)
+    e = cudaStreamSynchronize (s);
+  float ms = 0.0f;
+  if (e == cudaSuccess)
+    e = cudaEventElapsedTime (&ms, a, b);
+  if (a)
+    cudaEventDestroy (a);
+  if (b)
+    cudaEventDestroy (b);
+  cudaFree (st);
+  if (e != cudaSuccess)
+    return cuda_fail (e, "barrier self-test", __FILE__, __LINE__);
+  if (fault)
+    *fault = h.fault;
+  if (elapsed_s)
+    *elapsed_s = ms * 1e-3;
+  return BMFP_SUCCESS;
+}
 
 int raw_solve_grid (int64_t n, int *grid)
 {

@@ -191,6 +191,10 @@ constexpr int kRawParts = 9;
 
 // Grid of the phase kernels for n rows (the same rule as WideEngine).
 int raw_solve_grid (int64_t n, int *grid);
+// The persistent kernel's grid barrier made to time out on purpose (a wait
+// for one CTA more than the grid holds) after limit_s: reports the fault flag
+// the timed-out CTAs set and how long the launch took.
+int barrier_selftest (double limit_s, int *fault, double *elapsed_s, cudaStream_t s);
 int raw_jacobi (const RawSolve &b, cudaStream_t stream);
 int raw_start (const RawSolve &b, const void *d_rhs, double tol, int max_iter, cudaStream_t stream);
 int raw_phase (const RawSolve &b, int phase, cudaStream_t stream);

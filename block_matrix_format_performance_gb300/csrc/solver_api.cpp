@@ -501,6 +501,11 @@ int bmfp_solver_destroy (bmfp_solver_t sv)
   return BMFP_SUCCESS;
 }
 
+int bmfp_selftest_barrier_timeout (double limit_seconds, int *fault, double *elapsed_seconds, void *stream)
+{
+  return bmfp::barrier_selftest (limit_seconds, fault, elapsed_seconds, as_stream (stream));
+}
+
 } // extern "C"
 
 struct bmfp_batch_s

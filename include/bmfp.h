@@ -360,6 +360,14 @@ BMFP_API int bmfp_solver_create (bmfp_solver_t *out, bmfp_matrix_t A, const bmfp
 BMFP_API int bmfp_solver_solve (bmfp_solver_t s, const void *d_b, void *d_x, bmfp_solve_info *info,
                                 void *stream);
 BMFP_API int bmfp_solver_destroy (bmfp_solver_t s);
+/* Failure detection of the persistent iteration kernel, exercised without a
+ * fault: one cooperative launch whose grid barrier waits for one CTA more
+ * than the grid holds, so every CTA gives up after limit_seconds (0 < limit
+ * <= 1), records the fault and returns. *fault receives the flag the solver's
+ * host loop reads (1), *elapsed_seconds the launch's duration; the context
+ * stays usable. Synchronises the stream. */
+BMFP_API int bmfp_selftest_barrier_timeout (double limit_seconds, int *fault, double *elapsed_seconds,
+                                            void *stream);
 
 /* -------------------------------------------------------------- batched ---
  * Many independent square systems of uneven size solved by ONE persistent

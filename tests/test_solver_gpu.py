@@ -468,3 +468,22 @@ def test_persistent_launch_limits(lib, cuda):
     with pytest.raises(bm.BmfpError) as e:
         bm.Solver(A8, "fp64", launch_mode="persistent")
     assert e.value.status == bm.ERROR_NOT_SUPPORTED
+
+
+def test_grid_barrier_wait_runs_out_and_reports(lib, cuda):
+    """The persistent kernel's bounded barrier wait, run out on purpose: a
+    grid barrier waiting for one CTA more than the grid holds gives up after
+    its limit, records the fault the solver's host loop turns into
+    BMFP_ERROR_TIMEOUT, and the context stays usable (a persistent solve
+    right after it succeeds)."""
+    import ctypes
+    fault, elapsed = ctypes.c_int(0), ctypes.c_double(0.0)
+    st = lib.bmfp_selftest_barrier_timeout(0.05, ctypes.byref(fault), ctypes.byref(elapsed), None)
+    assert st == bm.SUCCESS, lib.bmfp_last_error()
+    assert fault.value == 1
+    assert 0.05 <= elapsed.value < 2.0
+    assert lib.bmfp_selftest_barrier_timeout(2.0, None, None, None) == bm.ERROR_INVALID_VALUE
+    rp, c, v, b = bm.gen_q4_elasticity(60, 15)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    x, info = bm.Solver(A, "fp64", launch_mode="persistent").solve_host(b)
+    assert info["status"] == bm.SUCCESS
