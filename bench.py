@@ -74,7 +74,7 @@ def parse_args():
                     help="skip timing the reference's own kernels on the sweep matrices")
     ap.add_argument("--no-solver", action="store_true", help="skip the batched-solve part of the line")
     ap.add_argument("--no-fem", action="store_true", help="skip the FEM solves (configs 0 and 2) of the line")
-    ap.add_argument("--no-serve", action="store_true", help="skip the served stream (config 4) of the line")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served request stream of the line")
     ap.add_argument("--serve-requests", type=int, default=5000, help="line: requests of the served stream")
     ap.add_argument("--sustained-requests", type=int, default=2500,
                     help="line: requests of the sustained-rate stream (the first of the same stream)")
@@ -523,14 +523,14 @@ def run_ours(args):
         solves = measure_batch(["fp64", "mixed"], 1e-10, 100000, 2)
         solves_shifted = measure_batch(["fp64", "mixed"], 1e-10, 100000, 2, shift=1e-3)
     # The FEM workloads of configs 0 and 2, the live cost of one solver
-    # iteration against its floors, and the served stream of config 4.
+    # iteration against its floors, and the served request stream.
     fem = None
     single = rank == 0 and world == 1  # the FEM and serving legs are one-GPU workloads
     if single and not args.no_fem:
         t0 = time.perf_counter()
-        fem = {"config0_200x50": fem_small(flush, stream),
+        fem = {"q4_200x50": fem_small(flush, stream),
                "iteration_roofline": [iteration_roofline(g, hbm, fp64_gflops) for g in ((1000, 250), (2000, 500))],
-               "config2_2000x500": fem_large(),
+               "q4_2000x500": fem_large(),
                "preconditioners": precond_compare(((1000, 250),), n_rhs=3)}
         fem["wall_s"] = round(time.perf_counter() - t0, 1)
     serve = None
@@ -866,7 +866,7 @@ def measure_batch(precisions, tol, max_iters, repeats, n_systems=256, per_reques
 
 
 def fem_small(flush, stream):
-    """BASELINE config 0: the 200x50 Q4 plane-stress operator (20 000 DOFs,
+    """The 200x50 Q4 plane-stress operator (20 000 DOFs,
     BCSR bs 2, FP64). SpMV with x uniform in [-1, 1] (seed 0) on the GPU
     (warm: 3.5 MB stays in L2, as in the reference's own back-to-back timing;
     and L2-flushed) and on the host (the reference CPU loop, 1 thread and all
@@ -1010,7 +1010,7 @@ def precond_compare(grids, n_rhs=3, tol=1e-10, max_iters=200000):
 
 
 def fem_large(cpu_iters=(12, 60)):
-    """BASELINE config 2: the Q4 operator on 2000x500 nodes (2 M DOFs, BCSR
+    """The Q4 operator on 2000x500 nodes (2 M DOFs, BCSR
     bs 2). Plain FP64 BiCGStab and FP32-inner / FP64-refined, both to 1e-10
     relative residual: iterations, time, true residual, the FP64 floor, and
     the mixed solution's error against the FP64 one. The CPU baseline runs
@@ -1201,7 +1201,7 @@ def fifo_timeline(arrivals, service):
 
 def serve_suite(n_requests, rate, precisions, sustained_factor, tol=1e-10, max_iters=100000, large_fraction=0.05,
                 sustained_requests=None):
-    """BASELINE config 4 in the bench line: the stream at the stated rate
+    """The served request stream in the bench line: the stream at the stated rate
     through the server in each precision; the same requests at a rate the
     server sustains (sustained_factor x the first server's throughput at
     the stated rate, so that arrivals do not outrun it; the same exponential
