@@ -73,7 +73,7 @@ def parse_args():
     ap.add_argument("--no-ref-variants", action="store_true",
                     help="skip timing the reference's own kernels on the sweep matrices")
     ap.add_argument("--no-solver", action="store_true", help="skip the batched-solve part of the line")
-    ap.add_argument("--no-fem", action="store_true", help="skip the FEM solves (configs 0 and 2) of the line")
+    ap.add_argument("--no-fem", action="store_true", help="skip the FEM solves (200x50, 2000x500) of the line")
     ap.add_argument("--no-serve", action="store_true", help="skip the served request stream of the line")
     ap.add_argument("--serve-requests", type=int, default=5000, help="line: requests of the served stream")
     ap.add_argument("--sustained-requests", type=int, default=2500,
@@ -102,6 +102,8 @@ def parse_args():
     ap.add_argument("--ndiag-dtype", default="f32", choices=("f32", "f64"))
     ap.add_argument("--systems", type=int, default=256, help="batch: number of systems")
     ap.add_argument("--batch-grid", default=None, help="batch: one NXxNY grid for every system (default: uneven)")
+    ap.add_argument("--batch-config", default=None,
+                    help="batch: CLUSTERxTHREADS for every precision instead of the autotuner's pick")
     ap.add_argument("--requests", type=int, default=1000, help="serve: number of requests")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (req/s)")
     ap.add_argument("--wide-lanes", type=int, default=None, help="serve: concurrent whole-GPU solves")
@@ -782,7 +784,8 @@ def fp64_floor(rp, c, v, bs, x, b):
     return float(2.0 ** -53 * np.linalg.norm(A @ np.abs(x)) / np.linalg.norm(b))
 
 
-def measure_batch(precisions, tol, max_iters, repeats, n_systems=256, per_request=True, grid=None, shift=None):
+def measure_batch(precisions, tol, max_iters, repeats, n_systems=256, per_request=True, grid=None, shift=None,
+                  config=None):
     """The uneven batch (nx log-uniform in [20, 400], ny = nx / 4, seeded): each
     precision solved by one persistent, graph-captured launch, and the plain
     FP64 per-request solver run system after system on the same GPU (its
@@ -812,7 +815,11 @@ def measure_batch(precisions, tol, max_iters, repeats, n_systems=256, per_reques
     for prec in precisions:
         batch = bm.Batch(mats, prec, tol=tol, max_iters=max_iters)
         t0 = time.perf_counter()
-        cluster, threads = batch.autotune(d_b, d_x, probe_iterations=1024)
+        if config:
+            cluster, threads = config
+            batch.configure(cluster, threads)
+        else:
+            cluster, threads = batch.autotune(d_b, d_x, probe_iterations=1024)
         tune_s = time.perf_counter() - t0
         batch.solve(d_b, d_x)
         times, infos = [], None
@@ -1067,8 +1074,9 @@ def run_batch(args):
     B.build()
     grid = tuple(int(t) for t in args.batch_grid.lower().split("x")) if args.batch_grid else None
     shift = args.shift if args.matrix == "shifted" else None
+    config = tuple(int(t) for t in args.batch_config.lower().split("x")) if args.batch_config else None
     res = measure_batch([args.precision], args.tol, args.max_iters, args.repeats, args.systems,
-                        per_request=args.repeats > 0, grid=grid, shift=shift)
+                        per_request=args.repeats > 0, grid=grid, shift=shift, config=config)
     print(json_line({"workload": "batch", "precision": args.precision,
                       "matrix": "q4" if shift is None else f"q4+{shift:g}I", **res}), flush=True)
 
