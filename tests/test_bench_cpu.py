@@ -63,3 +63,25 @@ def test_committed_traffic_names_the_lane_mapping():
     t = bench.committed_traffic("bcsr_native_bs32_f64_lanes65")
     assert t is not None and 6.0e9 < t < 7.0e9
     assert bench.committed_traffic("bcsr_native_bs32_f64_lanes64") is None
+
+
+def test_fifo_timeline_and_request_stream():
+    """The FIFO baseline's timeline (done_k = max(done_k-1, arrival_k) +
+    service_k) on a hand-checked case, and the seeded request stream:
+    deterministic, Poisson arrivals at the stated rate, grids as the uneven
+    batch plus the stated share of 1000x250 requests."""
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    import bench
+    t = bench.fifo_timeline([0.0, 0.5, 5.0], [1.0, 1.0, 2.0])
+    # done: 1.0, 2.0 (waits for the first), 7.0 (idle until 5.0); latencies 1.0, 1.5, 2.0
+    assert t["makespan_s"] == 7.0 and abs(t["solves_per_s"] - 3 / 7.0) < 0.01
+    assert t["latency_p50_s"] == 1.5
+    a1, g1 = bench.serve_stream(5000, 2000.0)
+    a2, g2 = bench.serve_stream(5000, 2000.0)
+    assert np.array_equal(a1, a2) and g1 == g2
+    assert np.all(np.diff(a1) > 0) and abs(len(a1) / a1[-1] - 2000.0) < 100.0
+    big = sum(g == (1000, 250) for g in g1)
+    assert 200 < big < 300  # 5 % of 5000
+    small = [g for g in g1 if g != (1000, 250)]
+    assert all(20 <= nx <= 400 and ny == max(2, round(nx / 4)) for nx, ny in small)
