@@ -387,8 +387,8 @@ def _same_bits(a, b):
     return a.dtype == b.dtype and np.array_equal(a.view(np.uint8), b.view(np.uint8))
 
 
-@pytest.mark.parametrize("case", ["q4", "q4_plain", "q4_jacobi", "q4_cps1", "q4_cps2", "csr", "bs3", "bs5",
-                                  "fp32", "mixed", "tiny"])
+@pytest.mark.parametrize("case", ["q4", "q4_plain", "q4_jacobi", "q4_cps1", "q4_cps2", "csr", "bs3", "bs4", "bs5",
+                                  "fp32", "fp32_jacobi", "mixed", "tiny"])
 def test_persistent_iterations_give_the_graphs_bits(lib, cuda, case):
     """The persistent kernel runs the phase bodies between grid barriers and
     derives the scalars in every CTA from the same partials, in the same
@@ -412,17 +412,19 @@ def test_persistent_iterations_give_the_graphs_bits(lib, cuda, case):
         crp, cc, cv = bm.bcsr_to_csr(rp, c, v, 2)
         A = bm.Matrix.from_csr(crp, cc, cv, len(crp) - 1)
         kw["preconditioner"] = "jacobi"
-    elif case in ("bs3", "bs5"):
+    elif case in ("bs3", "bs4", "bs5"):
         bs = int(case[2])
         rp, c, v = diag_dominant_bcsr(400, bs, seed=bs)
         b = np.random.default_rng(3).uniform(-1, 1, 400 * bs)
         A = bm.Matrix.from_bcsr(rp, c, v, bs)
-    elif case == "fp32":
+    elif case in ("fp32", "fp32_jacobi"):
         rp, c, v = diag_dominant_bcsr(500, 2, seed=9)
         b = np.random.default_rng(2).uniform(-1, 1, 1000).astype(np.float32)
         A = bm.Matrix.from_bcsr(rp, c, v.astype(np.float32), 2)
         precision = "fp32"
         kw["tol"] = 1e-5
+        if case == "fp32_jacobi":
+            kw["preconditioner"] = "jacobi"
     elif case == "mixed":
         rp, c, v = diag_dominant_bcsr(500, 2, seed=9)
         b = np.random.default_rng(2).uniform(-1, 1, 1000)
@@ -489,3 +491,28 @@ def test_grid_barrier_wait_runs_out_and_reports(lib, cuda):
     A = bm.Matrix.from_bcsr(rp, c, v, 2)
     x, info = bm.Solver(A, "fp64", launch_mode="persistent").solve_host(b)
     assert info["status"] == bm.SUCCESS
+
+
+def test_auto_launch_mode_takes_the_persistent_kernel_from_a_million_rows(lib, cuda):
+    """A 1 000 000-row system under the auto launch mode runs the persistent
+    kernel (its bits equal the explicit persistent launch's and, on the same
+    grid of 3 CTAs per SM, the graph's); a system just below runs graphs
+    (its bits equal the graph launch's at the default grid)."""
+    rp, c, v, b = bm.gen_q4_elasticity(1000, 500)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    out = {}
+    for mode in ("auto", "persistent", "graph"):
+        s = bm.Solver(A, "fp64", launch_mode=mode, ctas_per_sm=3, max_iters=200)
+        out[mode] = s.solve_host(b)
+        s.close()
+    assert out["auto"][1]["iterations"] == 200
+    assert _same_bits(out["auto"][0], out["persistent"][0]) and _same_bits(out["auto"][0], out["graph"][0])
+    A.close()
+    rp, c, v, b = bm.gen_q4_elasticity(999, 500)  # 999 000 rows
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    xa, _ = bm.Solver(A, "fp64", max_iters=100).solve_host(b)
+    xg, _ = bm.Solver(A, "fp64", launch_mode="graph", max_iters=100).solve_host(b)
+    xp, _ = bm.Solver(A, "fp64", launch_mode="persistent", max_iters=100).solve_host(b)
+    assert _same_bits(xa, xg)
+    assert not _same_bits(xa, xp)  # the persistent kernel's 3 CTAs per SM sum in another order
+    A.close()
