@@ -516,3 +516,37 @@ def test_auto_launch_mode_takes_the_persistent_kernel_from_a_million_rows(lib, c
     assert _same_bits(xa, xg)
     assert not _same_bits(xa, xp)  # the persistent kernel's 3 CTAs per SM sum in another order
     A.close()
+
+
+def test_concurrent_persistent_solves_on_separate_streams(lib, cuda):
+    """Three persistent solves of a 1 000 000-row system launched at once from
+    three host threads on three streams: cooperative launches that cannot be
+    resident together run one after another (no barrier gives up), and each
+    result has the bits of the same solve run alone."""
+    import threading
+    import torch
+    rp, c, v, b = bm.gen_q4_elasticity(1000, 500)
+    A = bm.Matrix.from_bcsr(rp, c, v, 2)
+    d_b = dev(b)
+    solo = torch.empty_like(d_b)
+    bm.Solver(A, "fp64", launch_mode="persistent", max_iters=160).solve(d_b, solo)
+    torch.cuda.synchronize()
+    out = {}
+
+    def worker(k):
+        st = torch.cuda.Stream()
+        x = torch.empty_like(d_b)
+        s = bm.Solver(A, "fp64", launch_mode="persistent", max_iters=160, stream=st.cuda_stream)
+        out[k] = (s.solve(d_b, x, stream=st.cuda_stream), x)
+        st.synchronize()
+
+    threads = [threading.Thread(target=worker, args=(k,)) for k in range(3)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert len(out) == 3
+    for info, x in out.values():
+        assert info["status"] == bm.ERROR_NOT_CONVERGED and info["iterations"] == 160, info  # the cap
+        assert torch.equal(x.view(torch.int64), solo.view(torch.int64))
+    A.close()
