@@ -2,33 +2,43 @@
 // (gpu/bicgstab.cu:387-513, optional point-Jacobi right preconditioning as in
 // :201-238), restructured for GB300.
 //
-// One iteration is five phase kernels over all rows, each a fixed persistent
-// grid; the scalars rho, alpha, omega live in device memory (DevState), so no
-// host round trip separates the phases (the reference did four blocking
-// copies and a print per iteration, gpu/bicgstab.cu:447-510):
+// One iteration is five phases over all rows on a fixed grid; the scalars
+// rho, alpha, omega, beta live in device memory (DevState), so no host round
+// trip separates the phases (the reference did four blocking copies and a
+// print per iteration, gpu/bicgstab.cu:447-510):
 //
-//   phase 1  rho = (rh, r), rr = (r, r)    from phase 5's partials
-//            convergence / breakdown test; beta = (rho/rho_prev)(alpha/omega)
-//            p = r + beta (p - omega v);   q = P p
+//   phase 1  p = r + beta (p - omega v);   q = P p
 //   phase 2  v = A q, partial (rh, v)       fused into the SpMV epilogue
-//   phase 3  alpha = rho / (rh, v);         s = r - alpha v;  z = P s
+//            -> alpha = rho / (rh, v)
+//   phase 3  s = r - alpha v;  z = P s
 //   phase 4  t = A z, partials (t, s), (t, t)
-//   phase 5  omega = (t, s) / (t, t);       x' += alpha q + omega z;  r = s - omega t
+//            -> omega = (t, s) / (t, t)
+//   phase 5  x' += alpha q + omega z;  r = s - omega t
 //            partials (rh, r), (r, r), (x', x')
+//            -> convergence, limit and breakdown tests, the replacement
+//               decision, beta = (rho / rho_prev)(alpha / omega)
 //
 // Algorithmic traffic per iteration: 2 SpMV + 17 n vector elements (no
-// preconditioner). Dot products are per-CTA partial sums written by one phase
-// and summed in a fixed order by every CTA of the next, so every CTA derives
-// bitwise the same scalar and a solve is deterministic for a given grid.
-// The host launches CUDA graphs of `chunk` iterations and only polls the
-// done flag between graphs; phases after convergence return immediately.
+// preconditioner). Each CTA reduces its threads' terms to one partial per dot
+// product; the CTA that finishes a phase last (an acq_rel arrival counter)
+// sums the grid's partials in index order and derives the scalars (the
+// arrows above), so a solve is deterministic for a given grid.
+//
+// The phases run in one of two ways, with the same bits on the same grid:
+// a CUDA graph of five kernels per iteration (`chunk` iterations per graph),
+// or one persistent cooperative kernel per `chunk` iterations whose phases
+// are separated by grid barriers, the last CTA to reach a barrier doing the
+// phase's scalar work (the auto choice from kPersistentRows rows). The host
+// only polls the done flag between launches; phases after convergence return
+// at once.
 //
 // Residual replacement with group update (van der Vorst and Ye 2000, see
-// DevState): phase 1 tracks the deviation bound and, when it is time,
-// replaces the p update of that iteration by the fold g += x', x' = 0; phase 2
-// of the same iteration then computes r = c - A g instead of v = A q (and
-// (rh, r), (r, r)), phases 3 and 4 return at once and phase 5 only marks the
-// replacement done. No kernel is added to the graph for it.
+// DevState): the decision at the end of phase 5 tracks the deviation bound
+// and, when it is time, the next iteration's phase 1 does the fold
+// g += x', x' = 0 instead of the p update; phase 2 then computes r = c - A g
+// instead of v = A q (and (rh, r), (r, r)), phases 3 and 4 return at once and
+// phase 5 only takes the decision on those sums. No kernel is added to the
+// graph for it.
 //
 // Differences from the reference, on purpose: the solution returned is the
 // last iterate (the reference copied buffer half 0, bicgstab.cu:515), the

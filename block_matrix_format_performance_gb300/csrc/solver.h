@@ -79,10 +79,13 @@ enum
   kStateBreakdown = 3
 };
 
-// Whole-GPU BiCGStab on one matrix: five fused phase kernels per iteration,
-// each over all rows with a fixed persistent grid, captured in a CUDA graph
-// of `chunk` iterations. Dot products are per-CTA partials summed in a fixed
-// order by the next phase, so a solve is deterministic for a given grid.
+// Whole-GPU BiCGStab on one matrix: five fused phases per iteration over all
+// rows on a fixed grid, either as phase kernels captured in a CUDA graph of
+// `chunk` iterations or as one persistent cooperative kernel per `chunk`
+// iterations with grid barriers between the phases (the same bits on the same
+// grid). Dot products are per-CTA partials summed in a fixed order by the
+// CTA that finishes the phase last, so a solve is deterministic for a given
+// grid.
 //
 // Every run solves A e = c from e = 0 (c = b for a fresh solve, c = the true
 // residual for a restart): the updates accumulate in xp, are folded into the
@@ -117,7 +120,8 @@ public:
   // (shadow_factor) instead of r0 itself, for a restart after a breakdown.
   int start_residual (const void *d_r, double tol, int max_iter_total, double norm_b,
                       cudaStream_t stream, int iter0 = -1, bool new_shadow = false);
-  // Runs graphs until the device sets done, then writes the run's result
+  // Runs graphs (or persistent launches) until the device sets done, then
+  // writes the run's result
   // into x; returns the final state. With d_snapshot, the run's iterate is
   // copied there each time the recursive residual has fallen 4x below the
   // last copy (and below snapshot_rr on entry), and *snapshot_rr receives
