@@ -1,7 +1,8 @@
 // Batched BiCGStab: many independent systems of uneven size in ONE persistent
 // launch (captured in a CUDA graph together with the work-queue reset).
 //
-// A "team" is a thread-block cluster (1, 2, 4 or 8 CTAs on as many SMs). Teams
+// A "team" is a thread-block cluster (1, 2, 4 or 8 CTAs; two CTAs of 512
+// threads fit an SM, so two teams share each SM's FP64 pipe). Teams
 // pull systems from a queue ordered largest first (longest-processing-time
 // scheduling) and run the whole solve of a system on their own: BiCGStab
 // phases separated by hardware cluster barriers, dot products reduced
